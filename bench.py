@@ -1,0 +1,428 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of the PBF solver step (4 iterations) on one GB300.
+
+Headline (`value`): the batched workload — 256 independent dam-break scenes,
+4k-64k particles each (log-uniform, seeded), advanced together by the batched
+engine (one CUDA-graph launch sequence per step).  Beside it (`plain`): the
+single large scene, 1,048,576 particles with a 2^21-cell table, through the
+plain single-scene step.  A "step" is one PBF step over the workload's
+synthetic input: each timed step re-loads the seeded initial state from HBM
+(device-to-device, inside the timed region) and runs the full step, so every
+step does identical work.  The configured physics (s_corr k = 0.1 at spacing
+0.5h) is not stable over many steps, so steps are not chained.
+
+`e2e`: the same step through the C ABI with HOST buffers: per step the
+packed positions and velocities go host->device from pinned memory, and the
+results come back device->host (pbf_batch_set_all / pbf_batch_get_all).
+
+`--impl reference`: the reference has no CPU implementation of its step; the
+reference arm times the CPU restatement of its algorithm (oracle/, OpenMP on
+all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (4 iters) batched vs plain, 1 GB300; p50/p99 scene latency"
+UNIT = "particle-steps/s"
+ITERS = 4
+# algorithmic bytes (design-independent compulsory traffic) per particle / per cell
+ALG_STEP_P = 192 + 88 * ITERS + 160      # + XSPH and vorticity (configured physics)
+ALG_STEP_C = 20 + 16 * ITERS + 24
+ALG_KERNEL = {  # per launch: (bytes per particle, bytes per cell)
+    "k_dp": (52, 8), "k_lambda": (36, 8), "k_neighbors_lambda": (36, 8),
+    "k_predict_hash": (52, 4), "k_xsph": (48, 8), "k_vort_omega": (48, 8), "k_vort_apply": (64, 8),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, workload: str):
+    """traffic_bytes_per_launch from profiles/<kernel>_<workload>.txt (ncu summary)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch"):
+                    return float(line.split("=")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def shard_scenes(n_scenes: int, rank: int, world: int):
+    """Replicas: every rank runs its own full batched workload with its own
+    seeds (weak scaling); no data-path collective."""
+    from ssf_pbf_cuda_gb300 import scenes
+    sc = scenes.config4(n_scenes)
+    if rank == 0:
+        return sc
+    # different seeds per rank, same size distribution
+    import numpy as np
+    rng = scenes.rng_for(4 + 7919 * rank)
+    out = []
+    for s in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(4096), math.log(65536)))))
+        out.append(scenes._random_scene(rng, 1000 + s + 100000 * rank, n))
+    del np
+    return out
+
+
+def cpu_baseline_sample(scs, params_fn, seconds: float = 10.0):
+    """The CPU oracle (OpenMP, all host threads) on the first scenes of the
+    workload until about `seconds` of work; returns (particle-steps/s, sample)."""
+    from oracle import oracle as O
+    O.build()
+    done, n_sc, t0 = 0, 0, time.perf_counter()
+    for sc in scs:
+        p = params_fn(sc)
+        b = O.Boundary(plane_pts=sc.planes[0], plane_nrm=sc.planes[1])
+        O.step(p, b, sc.area[0], sc.area[1], ITERS, sc.x, sc.v)
+        done += sc.n
+        n_sc += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, f"{n_sc} scenes ({done} particles), one step each, {dt:.1f} s", O.num_threads()
+
+
+def scene_params(sc):
+    from ssf_pbf_cuda_gb300 import api
+    p = sc.params(api.config_params())
+    p["grid_size"] = list(api.resolve_grid(p, sc.domain_end))
+    return p
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    scs = shard_scenes(args.scenes, 0, 1)
+    # bounded sample per step: scenes in order until ~1M particles
+    sample, tot = [], 0
+    for sc in scs:
+        sample.append(sc)
+        tot += sc.n
+        if tot >= args.ref_particles:
+            break
+    from oracle import oracle as O
+    O.build()
+    prepared = [(sc, scene_params(sc), O.Boundary(plane_pts=sc.planes[0], plane_nrm=sc.planes[1])) for sc in sample]
+
+    def one():
+        for sc, p, b in prepared:
+            O.step(p, b, sc.area[0], sc.area[1], ITERS, sc.x, sc.v)
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    dt = time.perf_counter() - t0
+    value = tot * args.steps / dt
+    cores = O.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded dam-break scenes)",
+        "config": {"workload": "batched: 256 dam-break scenes, 4k-64k particles (log-uniform), 4 iterations",
+                   "sample_particles": tot, "sample_scenes": len(sample)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"first {len(sample)} scenes ({tot} particles) of the batched workload, "
+                                   f"one step each per timed step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--ref-particles", type=int, default=1_000_000)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from ssf_pbf_cuda_gb300 import api, build
+    build.build()
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---------------- batched workload ----------------
+    scs = shard_scenes(args.scenes, rank, world)
+    params = [scene_params(sc) for sc in scs]
+    n_total = sum(sc.n for sc in scs)
+    cells = sum(int(np.prod(p["grid_size"])) + 1 for p in params)
+    batch = api.Batch(len(scs), n_total, cells, 30, device=local)
+    bnds = [api.Boundary(points_on_planes=sc.planes[0], normals_on_planes=sc.planes[1]) for sc in scs]
+    for sc, p, b in zip(scs, params, bnds):
+        batch.add_scene(p, sc.n, sc.domain_end, b, sc.area, sc.x, sc.v)
+    counts = np.array([sc.n for sc in scs], np.uint32)
+    x0h = np.concatenate([sc.x for sc in scs]).astype(np.float32)
+    v0h = np.concatenate([sc.v for sc in scs]).astype(np.float32)
+    x0d = torch.from_numpy(x0h).to(dev)
+    v0d = torch.from_numpy(v0h).to(dev)
+    torch.cuda.synchronize()
+    tile = args.tile or batch.autotune(ITERS, stream)
+    batch.set_tile(tile)
+
+    def batched_step():
+        batch.set_all(x0d, v0d, counts, stream)
+        batch.step(ITERS, stream)
+
+    for _ in range(args.warmup):
+        batched_step()
+    launches_per_step = batch.launches + 1  # + the unpack kernel of set_all
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            batched_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        nt = torch.tensor([float(n_total)], device=dev)
+        dist.all_reduce(nt)
+        job_particles = float(nt.item())
+    else:
+        job_particles = float(n_total)
+    value = job_particles * args.steps / (ms / 1e3)
+    flags = [batch.flags(i) for i in batch.scene_ids()]
+
+    # per-kernel timing (events between kernels, no graph) on the same input
+    prof = {}
+    for _ in range(3):
+        batch.set_all(x0d, v0d, counts, stream)
+        for name, t in batch.profile_step(ITERS, stream):
+            prof.setdefault(name, []).append(t)
+    per_kernel = {k: (statistics.mean(v), len(v) // 3) for k, v in prof.items()}
+    tot_by_kernel = {k: m * c for k, (m, c) in per_kernel.items()}
+    top = max(tot_by_kernel, key=tot_by_kernel.get)
+    peak, peak_kind = measured_peak_hbm()
+    bp, bc = ALG_KERNEL.get(top, (0, 0))
+    alg = bp * n_total + bc * cells
+    top_ms = per_kernel[top][0]
+    achieved = alg / (top_ms / 1e3) / 1e9
+    step_alg = ALG_STEP_P * n_total + ALG_STEP_C * cells
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": committed_traffic(top, "batched"),
+                "alg_bytes_per_launch": alg, "launch_ms": top_ms,
+                "step_alg_GBps": step_alg / (ms / args.steps / 1e3) / 1e9,
+                "kernel_share": {k: v / sum(tot_by_kernel.values()) for k, v in
+                                 sorted(tot_by_kernel.items(), key=lambda kv: -kv[1])}}
+
+    # ---------------- e2e through the C ABI with host buffers ----------------
+    e2e = None
+    if not args.no_e2e:
+        xh = torch.from_numpy(x0h).pin_memory()
+        vh = torch.from_numpy(v0h).pin_memory()
+        xo = torch.empty_like(xh).pin_memory()
+        vo = torch.empty_like(vh).pin_memory()
+        xhp, vhp, xop, vop = (t.numpy() for t in (xh, vh, xo, vo))
+
+        def e2e_step():
+            batch.set_all(xhp, vhp, counts, stream)
+            batch.step(ITERS, stream)
+            batch.get_all(xop, vop, stream)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": job_particles * args.steps / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(x0h.nbytes + v0h.nbytes), "d2h_bytes_per_step": int(x0h.nbytes + v0h.nbytes),
+               "ms_per_step": dt / args.steps * 1e3}
+
+    # ---------------- plain single large scene ----------------
+    plain = None
+    if not args.no_plain and rank == 0:
+        from ssf_pbf_cuda_gb300 import scenes
+        sc = scenes.config2()
+        p = scene_params(sc)
+        part = api.PbfParticle(p, sc.n, sc.domain_end, device=local)
+        b = api.Boundary(points_on_planes=sc.planes[0], normals_on_planes=sc.planes[1])
+        xd = torch.from_numpy(sc.x).to(dev)
+        vd = torch.from_numpy(sc.v).to(dev)
+
+        def plain_step():
+            part.set_particles(xd, vd, stream)
+            api.one_step(part, b, sc.area, ITERS, stream)
+
+        for _ in range(args.warmup):
+            plain_step()
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.steps):
+            plain_step()
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1) / args.steps
+        pprof = {}
+        for _ in range(3):
+            part.set_particles(xd, vd, stream)
+            for name, t in api.profile_step(part, b, sc.area, ITERS, stream):
+                pprof.setdefault(name, []).append(t)
+        pk = {k: statistics.mean(v) * (len(v) // 3) for k, v in pprof.items()}
+        ptop = max(pk, key=pk.get)
+        pcells = int(np.prod(p["grid_size"])) + 1
+        pbp, pbc = ALG_KERNEL.get(ptop, (0, 0))
+        pach = (pbp * sc.n + pbc * pcells) / (statistics.mean(pprof[ptop]) / 1e3) / 1e9
+        plain = {"value": sc.n / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
+                 "workload": "plain single scene: 1,048,576 particles (128x128x64 dam break), 2^21-cell table",
+                 "batched_over_plain": value / world / (sc.n / (pms / 1e3)),
+                 "top_kernel": ptop, "top_kernel_GBps": pach, "top_kernel_frac": pach / peak,
+                 "step_alg_GBps": (ALG_STEP_P * sc.n + ALG_STEP_C * pcells) / (pms / 1e3) / 1e9}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v_cpu, sample, cores = cpu_baseline_sample(scs, scene_params, 10.0)
+        cpu = {"value": v_cpu, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break scenes, no dataset)",
+            "config": {"workload": f"batched: {len(scs)} dam-break scenes per GPU, 4k-64k particles "
+                                   f"(log-uniform, seeded), {ITERS} iterations, s_corr k=0.1 n=4 dq=0.2h, "
+                                   "XSPH 0.01, vorticity 0.0005, eps 600, dt 1/120",
+                       "particles_per_gpu": n_total, "cells_per_gpu": cells, "tile": tile,
+                       "l2": "inputs larger than L2 (per-step working set >> 129 MB)",
+                       "step_definition": "device-resident initial state re-loaded, then one full step",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,982 @@
+// Host runtime of the PBF engine (see pbf_engine.h).
+#include "pbf_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace pbf103 {
+
+uint32_t blocks_per_sm(uint32_t tile);  // pbf_kernels.cu
+void set_last_error(const char *what, cudaError_t e);
+
+#define CK(call)                                      \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) {                      \
+            set_last_error(#call, e_);                \
+            return e_ == cudaErrorMemoryAllocation ? PBF_ERROR_OUT_OF_MEMORY : PBF_ERROR_CUDA; \
+        }                                             \
+    } while (0)
+
+// ------------------------------------------------------------ allocator --
+void RangeAllocator::reset(uint64_t size)
+{
+    size_ = size;
+    free_.clear();
+    used_.clear();
+    if (size) free_[0] = size;
+}
+
+bool RangeAllocator::alloc(uint64_t n, uint64_t *off)
+{
+    if (n == 0) {
+        *off = 0;
+        return true;
+    }
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            const uint64_t o = it->first, rem = it->second - n;
+            free_.erase(it);
+            if (rem) free_[o + n] = rem;
+            used_[o] = n;
+            *off = o;
+            return true;
+        }
+    }
+    return false;
+}
+
+void RangeAllocator::release(uint64_t off, uint64_t n)
+{
+    if (n == 0) return;
+    used_.erase(off);
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            free_.erase(it);
+        }
+    }
+}
+
+uint64_t RangeAllocator::high_water() const
+{
+    if (used_.empty()) return 0;
+    auto it = std::prev(used_.end());
+    return it->first + it->second;
+}
+
+uint64_t RangeAllocator::free_total() const
+{
+    uint64_t t = 0;
+    for (auto &kv : free_) t += kv.second;
+    return t;
+}
+
+// ----------------------------------------------------------- parameters --
+static float wpoly6_host(float r, float inv_h)
+{
+    const float q = r * inv_h;
+    const float alpha = 1.56668147065f * inv_h * inv_h * inv_h;
+    if (q <= 1.f) {
+        const float q2 = q * q;
+        const float t = 1.f - q2;
+        return alpha * t * t * t;
+    }
+    return 0.f;
+}
+
+static bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc *d, uint32_t grid[3])
+{
+    // pbf_particle::allocate rejects unset parameters (pbf_type.cpp:167-170);
+    // strictly positive values are required here because they are divided by.
+    if (!(p.stable_density > 0.f) || !(p.particle_mass > 0.f) || !(p.smoothing_length > 0.f) ||
+        !(p.time_step > 0.f) || p.stable_distance < 0.f)
+        return PBF_ERROR_BAD_PARAMETER;
+    if (p.max_pair_particle_num < 2 || p.max_pair_particle_num > 256) return PBF_ERROR_INVALID_ARGUMENT;
+    if (p.tensile_mode < 0 || p.tensile_mode > 2 || p.vorticity_mode < 0 || p.vorticity_mode > 2 ||
+        p.xsph_mode < 0 || p.xsph_mode > 1 || p.scorr_n < 0 || p.scorr_n > 16 || p.max_collision_passes == 0)
+        return PBF_ERROR_INVALID_ARGUMENT;
+    const float cw = p.cell_width > 0.f ? p.cell_width : p.smoothing_length;
+    uint32_t g[3];
+    if (p.grid_size[0] && p.grid_size[1] && p.grid_size[2]) {
+        for (int c = 0; c < 3; ++c) {
+            if (!is_pow2(p.grid_size[c]) || p.grid_size[c] > 4096) return PBF_ERROR_GRID_TOO_LARGE;
+            g[c] = p.grid_size[c];
+        }
+    } else {
+        if (!domain_end) return PBF_ERROR_INVALID_ARGUMENT;
+        if (pbf_calc_grid_size((double)cw * 2.0, domain_end, g) != PBF_SUCCESS) return PBF_ERROR_GRID_TOO_LARGE;
+    }
+    const uint64_t ncell = (uint64_t)g[0] * g[1] * g[2];
+    if (ncell >= (1ull << 31)) return PBF_ERROR_GRID_TOO_LARGE;
+    std::memset(d, 0, sizeof(*d));
+    d->gx = g[0];
+    d->gy = g[1];
+    d->gz = g[2];
+    d->ncell = (uint32_t)ncell;
+    d->cap = p.max_pair_particle_num - 1;
+    d->cw = cw;
+    const float h = p.smoothing_length;
+    const float inv_h = 1.f / h;
+    const float inv_h2 = inv_h * inv_h;
+    d->h = h;
+    d->h2 = h * h;
+    d->inv_h = inv_h;
+    d->alpha = 1.56668147065f * inv_h * inv_h2;
+    d->beta = -14.3239448745f * inv_h2 * inv_h2;
+    d->alpha6 = 1.56668147065f * inv_h * inv_h * inv_h;
+    d->m = p.particle_mass;
+    d->inv_rho0 = 1.f / p.stable_density;
+    d->m2rho2 = d->m * d->m * d->inv_rho0 * d->inv_rho0;
+    d->relax = p.relaxation;
+    d->dt = p.time_step;
+    d->inv_dt = 1.f / p.time_step;
+    // k = W(0.4h)^4, pow() evaluated in double then narrowed (pbf_solve.cpp:92,
+    // pbf_position_update.cu:232)
+    const float k = (float)std::pow((double)wpoly6_host(h * 0.4f, inv_h), 4);
+    d->inv_k = 1.f / k;
+    const float wdq = wpoly6_host(p.scorr_dq * h, inv_h);
+    d->inv_wdq = wdq > 0.f ? 1.f / wdq : 0.f;
+    d->scorr_k = p.scorr_k;
+    d->scorr_n = p.scorr_n;
+    d->tensile_mode = p.tensile_mode;
+    d->xsph_mode = p.xsph_mode;
+    d->vort_mode = p.vorticity_mode;
+    d->xsph_c = p.xsph_parameter;
+    d->vort_eps = p.vc_parameter;
+    for (int c = 0; c < 3; ++c) d->g[c] = p.body_force[c];
+    d->max_coll = p.max_collision_passes;
+    d->builtin_sphere = 1;
+    if (grid) std::memcpy(grid, g, sizeof(g));
+    return PBF_SUCCESS;
+}
+
+uint64_t bytes_per_particle(uint32_t max_pair)
+{
+    // x v xs xa xb xold w vt (float4) + key slot tmp perm + lam + nnb + nbr
+    return 8 * 16 + 4 * 4 + 4 + 1 + 4ull * (max_pair - 1);
+}
+
+// ---------------------------------------------------------------- batch --
+Batch::~Batch()
+{
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (cap_stream_) cudaStreamDestroy(cap_stream_);
+    if (small_done_) cudaEventDestroy(small_done_);
+    if (h_small_) cudaFreeHost(h_small_);
+    void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
+                    d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
+                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+}
+
+pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max_cells, uint32_t max_pair,
+                       int device)
+{
+    if (max_scenes == 0 || max_particles == 0 || max_cells == 0 || max_pair < 2 || max_pair > 256)
+        return PBF_ERROR_INVALID_ARGUMENT;
+    if (max_particles >= (1ull << 31) || max_cells >= (1ull << 32) - 8) return PBF_ERROR_INVALID_ARGUMENT;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PBF_ERROR_NO_DEVICE;
+    if (device < 0 || device >= ndev) return PBF_ERROR_INVALID_ARGUMENT;
+    device_ = device;
+    CK(cudaSetDevice(device_));
+    CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_));
+    max_scenes_ = max_scenes;
+    max_particles_ = max_particles;
+    max_cells_ = max_cells;
+    max_pair_ = max_pair;
+    bnd_capacity_ = (uint64_t)max_scenes * 32 + 1024;
+    max_tiles_ = max_particles / 64 + max_scenes + 1;
+    const uint64_t P = max_particles, C = max_cells;
+    auto A = [&](void **p, uint64_t bytes) -> cudaError_t {
+        arena_bytes_ += bytes;
+        return cudaMalloc(p, bytes ? bytes : 16);
+    };
+    CK(A((void **)&d_scenes_, sizeof(SceneDesc) * max_scenes));
+    CK(A((void **)&d_tile_scene_, 4 * max_tiles_));
+    CK(A((void **)&d_tile_start_, 4 * max_tiles_));
+    CK(A((void **)&d_ctrl_, sizeof(Ctrl)));
+    CK(A((void **)&d_scene_num_, 4ull * max_scenes));
+    CK(A((void **)&d_flags_, 4ull * max_scenes));
+    float4 **f4[] = {&d_x_, &d_v_, &d_xs_, &d_xa_, &d_xb_, &d_xold_, &d_w_, &d_vt_};
+    for (float4 **p : f4) CK(A((void **)p, 16 * P));
+    uint32_t **u4[] = {&d_key_, &d_slot_, &d_tmp_, &d_perm_};
+    for (uint32_t **p : u4) CK(A((void **)p, 4 * P));
+    CK(A((void **)&d_count_, 4 * (C + 4)));
+    CK(A((void **)&d_offsets_, 4 * (C + 4)));
+    CK(A((void **)&d_bsum_, 4 * ((C + kScanTile - 1) / kScanTile + 4)));
+    CK(A((void **)&d_lam_, 4 * P));
+    CK(A((void **)&d_nbr_, 4ull * (max_pair - 1) * P));
+    CK(A((void **)&d_nnb_, P));
+    CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
+    CK(A((void **)&d_pack_off_, 4ull * max_scenes));
+    CK(cudaMallocHost((void **)&h_small_, 8ull * max_scenes + 64));
+    CK(cudaEventCreateWithFlags(&small_done_, cudaEventDisableTiming));
+    CK(cudaMemset(d_count_, 0, 4 * (C + 4)));
+    CK(cudaMemset(d_offsets_, 0, 4 * (C + 4)));
+    CK(cudaMemset(d_scene_num_, 0, 4ull * max_scenes));
+    CK(cudaMemset(d_flags_, 0, 4ull * max_scenes));
+    CK(cudaMemset(d_ctrl_, 0, sizeof(Ctrl)));
+    CK(cudaMemset(d_nnb_, 0, P));
+    CK(cudaMemset(d_v_, 0, 16 * P));
+    CK(cudaMemset(d_x_, 0, 16 * P));
+    CK(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
+    palloc_.reset(P);
+    calloc_.reset(C);
+    balloc_.reset(bnd_capacity_);
+    bnd_host_.assign(bnd_capacity_, make_float4(0, 0, 0, 0));
+    scenes_.clear();
+    scenes_.reserve(max_scenes);
+    return PBF_SUCCESS;
+}
+
+uint32_t Batch::num_scenes() const
+{
+    uint32_t n = 0;
+    for (auto &s : scenes_) n += s.active ? 1 : 0;
+    return n;
+}
+
+const SceneHost *Batch::scene(uint32_t id) const
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return nullptr;
+    return &scenes_[id];
+}
+
+bool Batch::can_fit(uint32_t capacity, uint64_t cells, uint64_t bnd_len) const
+{
+    // conservative: the largest free block of each arena must hold the request
+    RangeAllocator p = palloc_, c = calloc_, b = balloc_;
+    uint64_t o;
+    return p.alloc(capacity, &o) && c.alloc(cells, &o) && b.alloc(bnd_len, &o) &&
+           (num_scenes() < max_scenes_);
+}
+
+static void fill_boundary(const pbf_boundary_t *b, std::vector<float4> &out)
+{
+    out.clear();
+    if (!b) return;
+    out = b->prims;
+}
+
+pbf_status Batch::add_scene(const pbf_params &p, uint32_t capacity, const float domain_end[3],
+                            const pbf_boundary_t *b, const float amin[3], const float amax[3], const float *x,
+                            const float *v, uint32_t n, bool src_dev, cudaStream_t st, uint32_t *id)
+{
+    if (capacity == 0 || n > capacity || !amin || !amax) return PBF_ERROR_INVALID_ARGUMENT;
+    if (p.max_pair_particle_num > max_pair_) return PBF_ERROR_INVALID_ARGUMENT;
+    SceneHost sh;
+    sh.params = p;
+    pbf_status rc = derive_desc(p, domain_end, &sh.desc, nullptr);
+    if (rc != PBF_SUCCESS) return rc;
+    uint32_t slot = UINT32_MAX;
+    for (uint32_t k = 0; k < scenes_.size(); ++k)
+        if (!scenes_[k].active) {
+            slot = k;
+            break;
+        }
+    if (slot == UINT32_MAX) {
+        if (scenes_.size() >= max_scenes_) return PBF_ERROR_CAPACITY;
+        slot = (uint32_t)scenes_.size();
+        scenes_.emplace_back();
+    }
+    std::vector<float4> prims;
+    fill_boundary(b, prims);
+    sh.cells = (uint64_t)sh.desc.ncell + 1;
+    sh.bnd_len = prims.size();
+    uint64_t po, co, bo;
+    if (!palloc_.alloc(capacity, &po)) return PBF_ERROR_OUT_OF_MEMORY;
+    if (!calloc_.alloc(sh.cells, &co)) {
+        palloc_.release(po, capacity);
+        return PBF_ERROR_OUT_OF_MEMORY;
+    }
+    if (!balloc_.alloc(sh.bnd_len, &bo)) {
+        palloc_.release(po, capacity);
+        calloc_.release(co, sh.cells);
+        return PBF_ERROR_OUT_OF_MEMORY;
+    }
+    sh.bnd_off = bo;
+    sh.desc.p_off = (uint32_t)po;
+    sh.desc.capacity = capacity;
+    sh.desc.c_off = (uint32_t)co;
+    sh.desc.b_off = (uint32_t)bo;
+    sh.desc.builtin_sphere = b ? 0u : 1u;
+    sh.desc.n_inner = b ? b->n_inner : 0;
+    sh.desc.n_outer = b ? b->n_outer : 0;
+    sh.desc.n_planes = b ? b->n_planes : 0;
+    for (int c = 0; c < 3; ++c) {
+        sh.desc.amin[c] = amin[c];
+        sh.desc.amax[c] = amax[c];
+    }
+    for (size_t k = 0; k < prims.size(); ++k) bnd_host_[bo + k] = prims[k];
+    sh.active = true;
+    sh.num_upper = 0;
+    scenes_[slot] = sh;
+    dirty_desc_ = dirty_tiles_ = true;
+    dirty_bnd_ = dirty_bnd_ || !prims.empty();
+    CK(cudaSetDevice(device_));
+    CK(cudaMemsetAsync(d_scene_num_ + slot, 0, 4, st));
+    CK(cudaMemsetAsync(d_flags_ + slot, 0, 4, st));
+    *id = slot;
+    if (n) {
+        rc = set_particles(slot, x, v, n, src_dev, false, st);
+        if (rc != PBF_SUCCESS) {
+            remove_scene(slot);
+            return rc;
+        }
+    }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::remove_scene(uint32_t id)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    SceneHost &s = scenes_[id];
+    palloc_.release(s.desc.p_off, s.desc.capacity);
+    calloc_.release(s.desc.c_off, s.cells);
+    balloc_.release(s.bnd_off, s.bnd_len);
+    s.active = false;
+    s.num_upper = 0;
+    dirty_desc_ = dirty_tiles_ = true;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_particles(uint32_t id, const float *x, const float *v, uint32_t n, bool src_dev,
+                                bool append, cudaStream_t st)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    if (n && !x) return PBF_ERROR_INVALID_ARGUMENT;
+    SceneHost &s = scenes_[id];
+    CK(cudaSetDevice(device_));
+    uint32_t start = 0;
+    if (append) {
+        pbf_status rc = get_num(id, &start, st);
+        if (rc != PBF_SUCCESS) return rc;
+    }
+    if ((uint64_t)start + n > s.desc.capacity) return PBF_ERROR_CAPACITY;
+    float4 *dx = d_x_ + s.desc.p_off + start;
+    float4 *dv = d_v_ + s.desc.p_off + start;
+    if (n) {
+        const float *sx = x, *sv = v;
+        if (!src_dev) {
+            // raw AoS float3 goes to the scene's slice of the xs / vt scratch
+            // (free between steps) and is widened on the device
+            float *stx = reinterpret_cast<float *>(d_xs_ + s.desc.p_off + start);
+            float *stv = reinterpret_cast<float *>(d_vt_ + s.desc.p_off + start);
+            CK(cudaMemcpyAsync(stx, x, 12ull * n, cudaMemcpyHostToDevice, st));
+            if (v) CK(cudaMemcpyAsync(stv, v, 12ull * n, cudaMemcpyHostToDevice, st));
+            sx = stx;
+            sv = v ? stv : nullptr;
+        }
+        launch_aos3_to_f4(sx, dx, n, st);
+        if (sv) launch_aos3_to_f4(sv, dv, n, st);
+        else CK(cudaMemsetAsync(dv, 0, 16ull * n, st));
+        CK(cudaGetLastError());
+    }
+    const uint32_t total = start + n;
+    launch_set_u32(d_scene_num_ + id, total, st);
+    CK(cudaGetLastError());
+    if (s.num_upper != total) dirty_tiles_ = true;
+    s.num_upper = total;
+    return PBF_SUCCESS;
+}
+
+void Batch::scene_ids(std::vector<uint32_t> &ids) const
+{
+    ids.clear();
+    for (uint32_t k = 0; k < scenes_.size(); ++k)
+        if (scenes_[k].active) ids.push_back(k);
+}
+
+pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float *v, bool src_dev, cudaStream_t st)
+{
+    CK(cudaSetDevice(device_));
+    std::vector<uint32_t> ids;
+    scene_ids(ids);
+    if (ids.empty()) return PBF_SUCCESS;
+    if (!x) return PBF_ERROR_INVALID_ARGUMENT;
+    for (size_t k = 0; k < ids.size(); ++k) {
+        const uint32_t c = counts ? counts[k] : scenes_[ids[k]].num_upper;
+        if (c > scenes_[ids[k]].desc.capacity) return PBF_ERROR_CAPACITY;
+    }
+    // the pinned scratch may still feed a previous copy
+    CK(cudaEventSynchronize(small_done_));
+    const size_t ns = scenes_.size();
+    uint32_t *pack = h_small_, *nums = h_small_ + max_scenes_;
+    std::memset(h_small_, 0, 8ull * max_scenes_);
+    uint64_t tot = 0;
+    for (size_t k = 0; k < ids.size(); ++k) {
+        SceneHost &s = scenes_[ids[k]];
+        const uint32_t c = counts ? counts[k] : s.num_upper;
+        pack[ids[k]] = (uint32_t)tot;
+        nums[ids[k]] = c;
+        tot += c;
+        if (s.num_upper != c) dirty_tiles_ = true;
+        s.num_upper = c;
+    }
+    CK(cudaMemcpyAsync(d_pack_off_, pack, 4 * ns, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_scene_num_, nums, 4 * ns, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(small_done_, st));
+    pbf_status rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    const float *sx = x, *sv = v;
+    if (!src_dev && tot) {
+        CK(cudaMemcpyAsync(d_xs_, x, 12 * tot, cudaMemcpyHostToDevice, st));
+        sx = reinterpret_cast<const float *>(d_xs_);
+        if (v) {
+            CK(cudaMemcpyAsync(d_vt_, v, 12 * tot, cudaMemcpyHostToDevice, st));
+            sv = reinterpret_cast<const float *>(d_vt_);
+        }
+    }
+    if (ctrl_.n_tiles) launch_unpack(args(), shape_for(tile_), d_pack_off_, sx, sv, st);
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::download_all(uint32_t *counts, float *x, float *v, bool dst_dev, cudaStream_t st)
+{
+    std::vector<uint32_t> nums, fl, ids;
+    pbf_status rc = read_all(nums, fl, false, st);
+    if (rc != PBF_SUCCESS) return rc;
+    scene_ids(ids);
+    if (ids.empty()) return PBF_SUCCESS;
+    CK(cudaEventSynchronize(small_done_));
+    uint32_t *pack = h_small_;
+    uint64_t tot = 0;
+    for (size_t k = 0; k < ids.size(); ++k) {
+        pack[ids[k]] = (uint32_t)tot;
+        if (counts) counts[k] = nums[ids[k]];
+        tot += nums[ids[k]];
+    }
+    CK(cudaMemcpyAsync(d_pack_off_, pack, 4 * scenes_.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(small_done_, st));
+    rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    if (!tot) return PBF_SUCCESS;
+    float *dx = x, *dv = v;
+    if (!dst_dev) {
+        dx = x ? reinterpret_cast<float *>(d_xs_) : nullptr;
+        dv = v ? reinterpret_cast<float *>(d_vt_) : nullptr;
+    }
+    launch_pack(args(), shape_for(tile_), d_pack_off_, dx, dv, st);
+    CK(cudaGetLastError());
+    if (!dst_dev) {
+        if (x) CK(cudaMemcpyAsync(x, dx, 12 * tot, cudaMemcpyDeviceToHost, st));
+        if (v) CK(cudaMemcpyAsync(v, dv, 12 * tot, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_scene_params(uint32_t id, const pbf_params &p)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    SceneHost &s = scenes_[id];
+    SceneDesc d;
+    uint32_t g[3];
+    pbf_params q = p;
+    // the hash grid is part of the allocation; keep it
+    q.grid_size[0] = s.desc.gx;
+    q.grid_size[1] = s.desc.gy;
+    q.grid_size[2] = s.desc.gz;
+    pbf_status rc = derive_desc(q, nullptr, &d, g);
+    if (rc != PBF_SUCCESS) return rc;
+    if (d.ncell != s.desc.ncell || q.max_pair_particle_num > max_pair_) return PBF_ERROR_INVALID_ARGUMENT;
+    d.p_off = s.desc.p_off;
+    d.capacity = s.desc.capacity;
+    d.c_off = s.desc.c_off;
+    d.b_off = s.desc.b_off;
+    d.builtin_sphere = s.desc.builtin_sphere;
+    d.n_inner = s.desc.n_inner;
+    d.n_outer = s.desc.n_outer;
+    d.n_planes = s.desc.n_planes;
+    for (int c = 0; c < 3; ++c) {
+        d.amin[c] = s.desc.amin[c];
+        d.amax[c] = s.desc.amax[c];
+    }
+    s.desc = d;
+    s.params = p;
+    dirty_desc_ = true;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_scene_boundary(uint32_t id, const pbf_boundary_t *b)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    SceneHost &s = scenes_[id];
+    std::vector<float4> prims;
+    fill_boundary(b, prims);
+    if (prims.size() != s.bnd_len) {
+        balloc_.release(s.bnd_off, s.bnd_len);
+        uint64_t bo;
+        if (!balloc_.alloc(prims.size(), &bo)) {
+            s.bnd_len = 0;
+            s.desc.builtin_sphere = 1;
+            return PBF_ERROR_OUT_OF_MEMORY;
+        }
+        s.bnd_off = bo;
+        s.bnd_len = prims.size();
+    }
+    for (size_t k = 0; k < prims.size(); ++k) bnd_host_[s.bnd_off + k] = prims[k];
+    s.desc.b_off = (uint32_t)s.bnd_off;
+    s.desc.builtin_sphere = b ? 0u : 1u;
+    s.desc.n_inner = b ? b->n_inner : 0;
+    s.desc.n_outer = b ? b->n_outer : 0;
+    s.desc.n_planes = b ? b->n_planes : 0;
+    dirty_desc_ = true;
+    dirty_bnd_ = true;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_scene_area(uint32_t id, const float amin[3], const float amax[3])
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    SceneHost &s = scenes_[id];
+    bool changed = false;
+    for (int c = 0; c < 3; ++c) {
+        changed |= s.desc.amin[c] != amin[c] || s.desc.amax[c] != amax[c];
+        s.desc.amin[c] = amin[c];
+        s.desc.amax[c] = amax[c];
+    }
+    if (changed) dirty_desc_ = true;
+    return PBF_SUCCESS;
+}
+
+void Batch::rebuild_tiles()
+{
+    tile_scene_.clear();
+    tile_start_.clear();
+    for (uint32_t k = 0; k < scenes_.size(); ++k) {
+        const SceneHost &s = scenes_[k];
+        if (!s.active) continue;
+        for (uint32_t st = 0; st < s.num_upper; st += tile_) {
+            tile_scene_.push_back(k);
+            tile_start_.push_back(st);
+        }
+    }
+    ctrl_.n_tiles = (uint32_t)tile_scene_.size();
+    ctrl_.n_cells = (uint32_t)calloc_.high_water();
+    ctrl_.n_scenes = (uint32_t)scenes_.size();
+}
+
+pbf_status Batch::upload(cudaStream_t st)
+{
+    CK(cudaSetDevice(device_));
+    if (dirty_desc_) {
+        std::vector<SceneDesc> h(scenes_.size());
+        for (size_t k = 0; k < scenes_.size(); ++k) h[k] = scenes_[k].desc;
+        if (!h.empty())
+            CK(cudaMemcpyAsync(d_scenes_, h.data(), sizeof(SceneDesc) * h.size(), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        dirty_desc_ = false;
+    }
+    if (dirty_bnd_) {
+        const uint64_t hw = balloc_.high_water();
+        if (hw) CK(cudaMemcpyAsync(d_bnd_, bnd_host_.data(), 16 * hw, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        dirty_bnd_ = false;
+    }
+    if (dirty_tiles_) {
+        rebuild_tiles();
+        if (tile_scene_.size() > max_tiles_) return PBF_ERROR_CAPACITY;
+        if (!tile_scene_.empty()) {
+            CK(cudaMemcpyAsync(d_tile_scene_, tile_scene_.data(), 4 * tile_scene_.size(), cudaMemcpyHostToDevice,
+                               st));
+            CK(cudaMemcpyAsync(d_tile_start_, tile_start_.data(), 4 * tile_start_.size(), cudaMemcpyHostToDevice,
+                               st));
+        }
+        CK(cudaMemcpyAsync(d_ctrl_, &ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        dirty_tiles_ = false;
+    }
+    return PBF_SUCCESS;
+}
+
+LaunchShape Batch::shape_for(uint32_t tile) const
+{
+    LaunchShape sh;
+    sh.tile = tile;
+    const uint32_t bps = std::max<uint32_t>(1, blocks_per_sm(tile));
+    const uint32_t full = (uint32_t)sms_ * bps;
+    const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
+    sh.grid = std::min(full, nt);
+    const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
+    sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
+    return sh;
+}
+
+StepArgs Batch::args() const
+{
+    StepArgs a;
+    a.scenes = d_scenes_;
+    a.tile_scene = d_tile_scene_;
+    a.tile_start = d_tile_start_;
+    a.ctrl = d_ctrl_;
+    a.scene_num = d_scene_num_;
+    a.flags = d_flags_;
+    a.x = d_x_;
+    a.v = d_v_;
+    a.xs = d_xs_;
+    a.key = d_key_;
+    a.slot = d_slot_;
+    a.tmp = d_tmp_;
+    a.perm = d_perm_;
+    a.count = d_count_;
+    a.offsets = d_offsets_;
+    a.bsum = d_bsum_;
+    a.xa = d_xa_;
+    a.xb = d_xb_;
+    a.xold = d_xold_;
+    a.lam = d_lam_;
+    a.nbr = d_nbr_;
+    a.nnb = d_nnb_;
+    a.w = d_w_;
+    a.vt = d_vt_;
+    a.bnd = d_bnd_;
+    a.nbr_stride = max_particles_;
+    return a;
+}
+
+pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
+{
+    const LaunchShape sh = shape_for(tile_);
+    bool xsph = false, vort = false;
+    for (auto &s : scenes_)
+        if (s.active) {
+            xsph |= s.desc.xsph_mode != 0;
+            vort |= s.desc.vort_mode != 0;
+        }
+    if (allow_graph && graph_mode_) {
+        GraphKey k;
+        k.iters = iters;
+        k.xsph = xsph;
+        k.vort = vort;
+        k.tile = sh.tile;
+        k.grid = sh.grid;
+        k.scan_grid = sh.scan_grid;
+        if (!exec_ || !(k == key_)) {
+            if (exec_) {
+                cudaGraphExecDestroy(exec_);
+                exec_ = nullptr;
+            }
+            CK(cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeThreadLocal));
+            graph_launches_ = enqueue_step(args(), sh, iters, xsph, vort, cap_stream_);
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamEndCapture(cap_stream_, &g));
+            cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                exec_ = nullptr;
+                set_last_error("cudaGraphInstantiate", e);
+                return PBF_ERROR_CUDA;
+            }
+            key_ = k;
+        }
+        CK(cudaGraphLaunch(exec_, st));
+        last_launches_ = graph_launches_;
+    } else {
+        last_launches_ = enqueue_step(args(), sh, iters, xsph, vort, st);
+    }
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
+namespace {
+struct EventHook : StepHook {
+    cudaStream_t st;
+    std::vector<cudaEvent_t> ev;
+    std::vector<std::string> names;
+    void launched(const char *name) override
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        ev.push_back(e);
+        names.emplace_back(name);
+    }
+};
+}  // namespace
+
+pbf_status Batch::profile_step(int iters, cudaStream_t st, float *ms, char *names, uint32_t max, uint32_t *n)
+{
+    if (iters < 0 || iters > 1000 || !n) return PBF_ERROR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(device_));
+    pbf_status rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    *n = 0;
+    if (ctrl_.n_tiles == 0) return PBF_SUCCESS;
+    bool xsph = false, vort = false;
+    for (auto &s : scenes_)
+        if (s.active) {
+            xsph |= s.desc.xsph_mode != 0;
+            vort |= s.desc.vort_mode != 0;
+        }
+    EventHook hook;
+    hook.st = st;
+    cudaEvent_t e0;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventRecord(e0, st));
+    last_launches_ = enqueue_step(args(), shape_for(tile_), iters, xsph, vort, st, &hook);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    cudaEvent_t prev = e0;
+    for (size_t k = 0; k < hook.ev.size(); ++k) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, prev, hook.ev[k]);
+        if (k < max) {
+            if (ms) ms[k] = t;
+            if (names) {
+                std::strncpy(names + 64 * k, hook.names[k].c_str(), 63);
+                names[64 * k + 63] = 0;
+            }
+        }
+        prev = hook.ev[k];
+    }
+    *n = (uint32_t)std::min<size_t>(hook.ev.size(), max);
+    for (auto e : hook.ev) cudaEventDestroy(e);
+    cudaEventDestroy(e0);
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::step(int iters, cudaStream_t st)
+{
+    if (iters < 0 || iters > 1000) return PBF_ERROR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(device_));
+    pbf_status rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    if (ctrl_.n_tiles == 0) {
+        last_launches_ = 0;
+        return PBF_SUCCESS;
+    }
+    return run(iters, st, true);
+}
+
+pbf_status Batch::get_num(uint32_t id, uint32_t *num, cudaStream_t st)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    CK(cudaSetDevice(device_));
+    uint32_t n = 0;
+    CK(cudaMemcpyAsync(&n, d_scene_num_ + id, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (n != scenes_[id].num_upper) {
+        scenes_[id].num_upper = n;
+        dirty_tiles_ = true;
+    }
+    *num = n;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::get_particles(uint32_t id, float *x, float *v, uint32_t *num, bool dst_dev, cudaStream_t st)
+{
+    uint32_t n = 0;
+    pbf_status rc = get_num(id, &n, st);
+    if (rc != PBF_SUCCESS) return rc;
+    if (num) *num = n;
+    if (!n) return PBF_SUCCESS;
+    const SceneHost &s = scenes_[id];
+    float *stage = reinterpret_cast<float *>(d_xs_ + s.desc.p_off);  // xs is free between steps
+    float4 *srcs[2] = {d_x_ + s.desc.p_off, d_v_ + s.desc.p_off};
+    float *dsts[2] = {x, v};
+    for (int k = 0; k < 2; ++k) {
+        if (!dsts[k]) continue;
+        if (dst_dev) {
+            launch_f4_to_aos3(srcs[k], dsts[k], n, st);
+            CK(cudaGetLastError());
+        } else {
+            launch_f4_to_aos3(srcs[k], stage, n, st);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(dsts[k], stage, 12ull * n, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::get_flags(uint32_t id, uint32_t *flags, bool clear, cudaStream_t st)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    CK(cudaSetDevice(device_));
+    uint32_t f = 0;
+    CK(cudaMemcpyAsync(&f, d_flags_ + id, 4, cudaMemcpyDeviceToHost, st));
+    if (clear) CK(cudaMemsetAsync(d_flags_ + id, 0, 4, st));
+    CK(cudaStreamSynchronize(st));
+    *flags = f;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::read_all(std::vector<uint32_t> &nums, std::vector<uint32_t> &flags, bool clear_flags,
+                           cudaStream_t st)
+{
+    CK(cudaSetDevice(device_));
+    const size_t n = scenes_.size();
+    nums.assign(n, 0);
+    flags.assign(n, 0);
+    if (!n) return PBF_SUCCESS;
+    CK(cudaMemcpyAsync(nums.data(), d_scene_num_, 4 * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(flags.data(), d_flags_, 4 * n, cudaMemcpyDeviceToHost, st));
+    if (clear_flags) CK(cudaMemsetAsync(d_flags_, 0, 4 * n, st));
+    CK(cudaStreamSynchronize(st));
+    for (size_t k = 0; k < n; ++k)
+        if (scenes_[k].active && scenes_[k].num_upper != nums[k]) {
+            scenes_[k].num_upper = nums[k];
+            dirty_tiles_ = true;
+        }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::get_debug(uint32_t id, uint32_t *sorted_hash, uint32_t *perm, uint32_t *cell_start,
+                            uint32_t *cell_end, uint32_t *neighbor_list, uint32_t *n_in_out, cudaStream_t st)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    CK(cudaSetDevice(device_));
+    CK(cudaStreamSynchronize(st));
+    const SceneDesc &d = scenes_[id].desc;
+    const uint64_t C = d.ncell;
+    std::vector<uint32_t> off(C + 2);
+    CK(cudaMemcpy(off.data(), d_offsets_ + d.c_off, 4 * (C + 2), cudaMemcpyDeviceToHost));
+    const uint32_t base = off[0];
+    const uint32_t n_in = off[C + 1] - base;
+    const uint32_t live = off[C] - base;
+    if (n_in_out) *n_in_out = n_in;
+    std::vector<uint32_t> key(n_in), pm(n_in);
+    if (n_in) {
+        CK(cudaMemcpy(key.data(), d_key_ + d.p_off, 4ull * n_in, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(pm.data(), d_perm_ + d.p_off, 4ull * n_in, cudaMemcpyDeviceToHost));
+    }
+    if (perm) std::memcpy(perm, pm.data(), 4ull * n_in);
+    if (sorted_hash)
+        for (uint32_t p = 0; p < n_in; ++p) sorted_hash[p] = key[pm[p]];
+    if (cell_start || cell_end)
+        for (uint64_t c = 0; c < C; ++c) {
+            const bool empty = off[c] == off[c + 1];
+            if (cell_start) cell_start[c] = empty ? 0xFFFFFFFFu : off[c] - base;
+            if (cell_end) cell_end[c] = empty ? 0xFFFFFFFFu : off[c + 1] - base;
+        }
+    if (neighbor_list) {
+        const uint32_t mp = d.cap + 1;
+        const uint64_t padded = ((uint64_t)live + 31) / 32 * 32;
+        std::fill(neighbor_list, neighbor_list + padded * mp, 0xFFFFFFFFu);
+        std::vector<uint8_t> nn(live);
+        std::vector<uint32_t> row(live);
+        if (live) CK(cudaMemcpy(nn.data(), d_nnb_ + d.p_off, live, cudaMemcpyDeviceToHost));
+        for (uint32_t k = 0; k < d.cap && live; ++k) {
+            CK(cudaMemcpy(row.data(), d_nbr_ + (uint64_t)k * max_particles_ + d.p_off, 4ull * live,
+                          cudaMemcpyDeviceToHost));
+            for (uint32_t p = 0; p < live; ++p)
+                if (k < nn[p])
+                    neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp] = row[p] - d.p_off;
+        }
+    }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::import_x_device(uint32_t id, const float *x_dev, uint32_t n, cudaStream_t st)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    if (n > scenes_[id].desc.capacity) return PBF_ERROR_CAPACITY;
+    launch_aos3_to_f4(x_dev, d_x_ + scenes_[id].desc.p_off, n, st);
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::export_x_device(uint32_t id, float *x_dev, cudaStream_t st)
+{
+    uint32_t n = 0;
+    pbf_status rc = get_num(id, &n, st);
+    if (rc != PBF_SUCCESS) return rc;
+    launch_f4_to_aos3(d_x_ + scenes_[id].desc.p_off, x_dev, n, st);
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_tile(uint32_t tile)
+{
+    if (tile != 64 && tile != 128 && tile != 256 && tile != 512) return PBF_ERROR_INVALID_ARGUMENT;
+    if (tile != tile_) {
+        tile_ = tile;
+        dirty_tiles_ = true;
+    }
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
+{
+    CK(cudaSetDevice(device_));
+    pbf_status rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    if (ctrl_.n_tiles == 0) {
+        if (chosen) *chosen = tile_;
+        return PBF_SUCCESS;
+    }
+    const uint64_t hw = palloc_.high_water();
+    float4 *sx = nullptr, *sv = nullptr;
+    uint32_t *sn = nullptr, *sf = nullptr;
+    CK(cudaMalloc(&sx, 16 * std::max<uint64_t>(hw, 1)));
+    CK(cudaMalloc(&sv, 16 * std::max<uint64_t>(hw, 1)));
+    CK(cudaMalloc(&sn, 4ull * max_scenes_));
+    CK(cudaMalloc(&sf, 4ull * max_scenes_));
+    auto save = [&]() -> cudaError_t {
+        cudaMemcpyAsync(sx, d_x_, 16 * hw, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(sv, d_v_, 16 * hw, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(sn, d_scene_num_, 4ull * max_scenes_, cudaMemcpyDeviceToDevice, st);
+        return cudaMemcpyAsync(sf, d_flags_, 4ull * max_scenes_, cudaMemcpyDeviceToDevice, st);
+    };
+    auto restore = [&]() -> cudaError_t {
+        cudaMemcpyAsync(d_x_, sx, 16 * hw, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(d_v_, sv, 16 * hw, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(d_scene_num_, sn, 4ull * max_scenes_, cudaMemcpyDeviceToDevice, st);
+        return cudaMemcpyAsync(d_flags_, sf, 4ull * max_scenes_, cudaMemcpyDeviceToDevice, st);
+    };
+    CK(save());
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const uint32_t cands[] = {128, 256, 512, 64};
+    uint32_t best = tile_;
+    float best_ms = 1e30f;
+    const uint32_t orig = tile_;
+    for (uint32_t t : cands) {
+        set_tile(t);
+        rc = upload(st);
+        if (rc != PBF_SUCCESS) break;
+        run(iters, st, false);  // warm-up
+        CK(cudaEventRecord(e0, st));
+        for (int r = 0; r < 3; ++r) run(iters, st, false);
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = t;
+        }
+        CK(restore());
+    }
+    (void)orig;
+    set_tile(best);
+    rc = upload(st);
+    CK(cudaStreamSynchronize(st));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sx);
+    cudaFree(sv);
+    cudaFree(sn);
+    cudaFree(sf);
+    if (chosen) *chosen = best;
+    return rc;
+}
+
+}  // namespace pbf103

@@ -1,0 +1,119 @@
+// Internal interfaces between the host runtime (pbf_engine.cu) and the
+// device kernels (pbf_kernels.cu).  Not part of the C ABI.
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <cuda_runtime.h>
+
+namespace pbf103 {
+
+// Per-scene constants, one 192-byte record per scene slot in device memory.
+// Derived once on the host from pbf_params (the reference keeps these in
+// __constant__ symbols and a function-static, pbf_position_update.cu:14-17,
+// pbf_solve.cpp:92; here they are per scene so scenes never share state).
+struct SceneDesc {
+    uint32_t p_off;      // first particle slot of the scene in the flat arrays
+    uint32_t capacity;   // particle slots owned by the scene
+    uint32_t c_off;      // first cell of the scene in the flat cell arrays
+    uint32_t ncell;      // Gx*Gy*Gz; cell ncell (local) is the deleted bucket
+    uint32_t gx, gy, gz; // power-of-two hash grid
+    uint32_t cap;        // neighbour slots usable (max_pair - 1)
+    float cw;            // cell width
+    float h2;            // h*h, neighbour acceptance
+    float inv_h;         // 1/h
+    float alpha;         // poly6 factor 1.56668147065 / h^3
+    float beta;          // spiky-derivative factor -14.3239448745 / h^4
+    float m;             // particle mass
+    float inv_rho0;      // 1 / rest density
+    float m2rho2;        // m^2 / rho0^2
+    float relax;         // CFM epsilon
+    float dt;
+    float inv_dt;
+    float inv_k;         // reference s_corr: 1 / W(0.4h)^4
+    float inv_wdq;       // textbook s_corr: 1 / W(dq h)
+    float scorr_k;
+    int32_t scorr_n;
+    int32_t tensile_mode;
+    int32_t xsph_mode;
+    int32_t vort_mode;
+    float xsph_c;
+    float vort_eps;
+    float alpha6;        // 1.56668147065 * inv_h * inv_h * inv_h (Wpoly6 order)
+    float h;
+    float g[3];
+    uint32_t max_coll;
+    float amin[3];
+    uint32_t b_off;      // first float4 of the scene's boundary primitives
+    float amax[3];
+    uint32_t n_inner;
+    uint32_t n_outer;
+    uint32_t n_planes;
+    uint32_t builtin_sphere;
+    uint32_t pad0, pad1, pad2;
+};
+static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
+
+// Device-resident launch control; lets a captured graph run on a scene set
+// that changes between launches.
+struct Ctrl {
+    uint32_t n_tiles;    // tiles in tile_scene/tile_start
+    uint32_t n_cells;    // cell entries to scan (high-water mark of cell ranges)
+    uint32_t n_scenes;
+    uint32_t pad;
+};
+
+struct StepArgs {
+    const SceneDesc *scenes;
+    const uint32_t *tile_scene;   // tile -> scene
+    const uint32_t *tile_start;   // tile -> first local particle index
+    const Ctrl *ctrl;
+    uint32_t *scene_num;          // particles per scene at step start
+    uint32_t *flags;              // per-scene PBF_FLAG_* words
+    float4 *x, *v;                // particle phase (sorted after each step)
+    float4 *xs;                   // predicted positions, input order
+    uint32_t *key, *slot, *tmp, *perm;
+    uint32_t *count, *offsets, *bsum;
+    float4 *xa, *xb, *xold;       // working positions (ping-pong) and sorted old x
+    float *lam;
+    uint32_t *nbr;                // nbr[k * nbr_stride + i]
+    uint8_t *nnb;
+    float4 *w, *vt;               // vorticity, XSPH velocity scratch
+    const float4 *bnd;            // boundary primitives
+    uint64_t nbr_stride;
+};
+
+struct LaunchShape {
+    uint32_t tile;        // particles per tile = threads per block
+    uint32_t grid;        // persistent grid (blocks) for tile kernels
+    uint32_t scan_grid;   // grid for the scan kernels
+};
+
+// Called after every kernel launch of a step (per-kernel event timing).
+struct StepHook {
+    virtual void launched(const char *kernel_name) = 0;
+    virtual ~StepHook() = default;
+};
+
+// Enqueue one full solver step for every scene in the tile list.
+// Returns the number of kernels launched.
+uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, bool xsph, bool vort,
+                      cudaStream_t stream, StepHook *hook = nullptr);
+
+// Edge conversions between the ABI's AoS float3 and the internal float4.
+void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st);
+void launch_f4_to_aos3(const float4 *src, float *dst, uint32_t n, cudaStream_t st);
+void launch_set_u32(uint32_t *dst, uint32_t value, cudaStream_t st);
+// Whole-batch moves between a packed AoS float3 buffer (active scenes in
+// slot order, pack_off[s] = first packed particle of scene s) and the
+// scene-sliced float4 phase arrays.  unpack uses the tile list (counts must
+// already be in scene_num); pack writes the scene_num[s] first particles.
+void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, const float *src_x,
+                   const float *src_v, cudaStream_t st);
+void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, float *dst_x, float *dst_v,
+                 cudaStream_t st);
+
+constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
+constexpr uint32_t kScanWarps = 8;
+constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells per scan tile
+
+}  // namespace pbf103

@@ -1,0 +1,867 @@
+// Device kernels of the PBF solver step (sm_103a).
+//
+// One thread per particle; blocks walk a device-resident tile list in a
+// grid-stride loop, each tile belonging to one scene, so the same kernels run
+// a single scene (the plain step) or hundreds of scenes (the batched engine)
+// with a fixed launch shape that a CUDA graph can capture once.
+//
+// Data layout (flat arrays over every scene's particle slots):
+//   x, v, xs, xa, xb, xold, w, vt : float4 (xyz + unused w), 16-byte aligned
+//   key, slot, tmp, perm          : uint32 per particle
+//   nbr                           : uint32 [slot k][particle i] (coalesced per k)
+//   count / offsets               : uint32 per cell (+1 deleted bucket per scene)
+//
+// Integer work (predict, cell hash, stable counting sort, neighbour
+// acceptance) uses explicitly rounded intrinsics so that it is bit-exact
+// against the CPU oracle.  Floating-point solver math follows the reference's
+// operation order but uses rsqrtf (as the reference does).
+#include "pbf_internal.h"
+#include "pbf103.h"
+
+namespace pbf103 {
+namespace {
+
+// ---------------------------------------------------------------- helpers --
+
+// static_cast<int>(floor(p / cell_width)), src/pbf/interaction/cuda/pbf_grid.h:20-33,
+// with IEEE division (the reference build used -prec-div=false).
+__device__ __forceinline__ int32_t cell_coord(float p, float cw)
+{
+    return __float2int_rd(__fdiv_rn(p, cw));
+}
+
+// calcGridHash with power-of-two wrap, pbf_grid.h:53-61.
+__device__ __forceinline__ uint32_t hash3(uint32_t x, uint32_t y, uint32_t z, const SceneDesc &d)
+{
+    x &= d.gx - 1u;
+    y &= d.gy - 1u;
+    z &= d.gz - 1u;
+    return z * d.gx * d.gy + y * d.gx + x;
+}
+
+// r^2 exactly as findPair computes it (pbf_neighbor_search_util.cu:398):
+// fmaf(dz, dz, fmaf(dy, dy, dx * dx)), no further contraction.
+__device__ __forceinline__ float dist2_exact(float4 a, float4 b)
+{
+    const float d0 = __fsub_rn(a.x, b.x), d1 = __fsub_rn(a.y, b.y), d2 = __fsub_rn(a.z, b.z);
+    return __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
+}
+
+// Kernel value and gradient for a listed pair at current positions:
+// memorizeKernelPair, src/pbf/solver/cuda/pbf_kernel_memorization.cu:14-56.
+struct PairK {
+    float W;
+    float gx, gy, gz;
+};
+
+__device__ __forceinline__ PairK pair_kernel(float4 xi, float4 xj, float inv_h, float alpha, float beta)
+{
+    PairK o;
+    const float d0 = xi.x - xj.x, d1 = xi.y - xj.y, d2 = xi.z - xj.z;
+    const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
+    const float inv_r = rsqrtf(r2);
+    const float q2 = r2 * inv_h * inv_h;
+    o.W = 0.f;
+    if (q2 <= 1.f) {
+        const float t = 1.f - q2;
+        o.W = alpha * t * t * t;
+    }
+    const float r = r2 * inv_r;
+    const float u = fmaf(-r, inv_h, 1.f);
+    const float kd = (inv_h <= inv_r) ? beta * u * u : 0.f;
+    o.gx = o.gy = o.gz = 0.f;
+    if (r2 > 0.f) {
+        const float s = kd * inv_r;
+        o.gx = s * d0;
+        o.gy = s * d1;
+        o.gz = s * d2;
+    }
+    return o;
+}
+
+// Wpoly6 / WspikyDerivative, src/pbf/kernel/cuda/detail/pbf_kernel.inl:34-63.
+__device__ __forceinline__ float wpoly6(float r, float inv_h, float alpha6)
+{
+    const float q = r * inv_h;
+    if (q <= 1.f) {
+        const float t = 1.f - q * q;
+        return alpha6 * t * t * t;
+    }
+    return 0.f;
+}
+
+__device__ __forceinline__ float wspiky_d(float r, float kinv_h)
+{
+    const float q = r * kinv_h;
+    if (q <= 1.f) {
+        const float ih2 = kinv_h * kinv_h;
+        const float t = 1.f - q;
+        return -14.3239448745f * (ih2 * ih2) * t * t;
+    }
+    return 0.f;
+}
+
+// responseInnerSphereBoundary, src/pbf/solver/cuda/boundary/pbf_sphere_boundary.cu:8-34
+__device__ __forceinline__ void inner_sphere(bool &hit, float3 &dp, float3 p, float4 s)
+{
+    const float c0 = s.x - p.x, c1 = s.y - p.y, c2 = s.z - p.z;
+    const float d2 = fmaf(c2, c2, fmaf(c1, c1, c0 * c0));
+    const float rinv = rsqrtf(d2);
+    if (d2 > s.w * s.w) {
+        hit = true;
+        dp.x = fmaf(c0, 1.0001f, dp.x);
+        dp.y = fmaf(c1, 1.0001f, dp.y);
+        dp.z = fmaf(c2, 1.0001f, dp.z);
+        dp.x = fmaf(-s.w, c0 * rinv, dp.x);
+        dp.y = fmaf(-s.w, c1 * rinv, dp.y);
+        dp.z = fmaf(-s.w, c2 * rinv, dp.z);
+    }
+}
+
+// responsePlaneBoundary, src/pbf/solver/cuda/boundary/pbf_plane_boundary.cu:6-45
+__device__ __forceinline__ void plane(bool &hit, float3 &dp, float3 o, float3 p, float4 on, float4 n)
+{
+    const float pa0 = o.x - on.x, pa1 = o.y - on.y, pa2 = o.z - on.z;
+    const float pb0 = p.x - on.x, pb1 = p.y - on.y, pb2 = p.z - on.z;
+    const float pa_n = fmaf(pa2, n.z, fmaf(pa1, n.y, pa0 * n.x));
+    const float pb_n = fmaf(pb2, n.z, fmaf(pb1, n.y, pb0 * n.x));
+    float3 is;
+    if (pa_n == 0.f && pb_n == 0.f) {
+        return;
+    } else if (pa_n >= 0.f && pb_n < 0.f) {
+        hit = true;
+        const float f = fabsf(pa_n) / (fabsf(pa_n) + fabsf(pb_n));
+        is.x = o.x + (p.x - o.x) * f;
+        is.y = o.y + (p.y - o.y) * f;
+        is.z = o.z + (p.z - o.z) * f;
+    } else if (pa_n < 0.f && pb_n < 0.f) {
+        hit = true;
+        const float dd = -fmaf(on.z, n.z, fmaf(on.y, n.y, on.x * n.x));
+        const float t = -(fmaf(p.z, n.z, fmaf(p.y, n.y, p.x * n.x)) + dd) / fmaf(n.z, n.z, fmaf(n.y, n.y, n.x * n.x));
+        is.x = p.x + t * n.x;
+        is.y = p.y + t * n.y;
+        is.z = p.z + t * n.z;
+    } else {
+        return;
+    }
+    const float di0 = p.x - is.x, di1 = p.y - is.y, di2 = p.z - is.z;
+    const float c = fmaf(di2, n.z, fmaf(di1, n.y, di0 * n.x));
+    dp.x += -c * n.x;
+    dp.y += -c * n.y;
+    dp.z += -c * n.z;
+}
+
+// responseCollisionCUDA, src/pbf/solver/cuda/pbf_response_collision.cu:12-66 (and the
+// fixed-sphere variant, pbf_constraint.cu:262-315).  old_x is the current
+// position, as in the reference (pbf_response_collision.cu:31).  The
+// reference repeats until no primitive reports a hit; here at most max_coll
+// passes.  Returns false when the bound was reached.
+__device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, float3 x, float3 &dp)
+{
+    for (uint32_t pass = 0; pass < d.max_coll; ++pass) {
+        float3 p = make_float3(x.x + dp.x, x.y + dp.y, x.z + dp.z);
+        bool hit = false;
+        if (d.builtin_sphere) {
+            inner_sphere(hit, dp, p, make_float4(3.f, 3.f, 3.f, 3.f));
+        } else {
+            const float4 *b = bnd + d.b_off;
+            const uint32_t ns = d.n_inner + d.n_outer;  // outer spheres use the inner routine
+            for (uint32_t k = 0; k < ns; ++k) {
+                inner_sphere(hit, dp, p, __ldg(b + k));
+                p = make_float3(x.x + dp.x, x.y + dp.y, x.z + dp.z);
+            }
+            b += ns;
+            for (uint32_t k = 0; k < d.n_planes; ++k) {
+                plane(hit, dp, x, p, __ldg(b + 2 * k), __ldg(b + 2 * k + 1));
+                p = make_float3(x.x + dp.x, x.y + dp.y, x.z + dp.z);
+            }
+        }
+        if (!hit) return true;
+    }
+    return false;
+}
+
+// Visit the particles of the 27 cells around xp in the reference's order
+// (z, y, x from -1 to 1; ascending sorted index inside a cell,
+// pbf_neighbor_search_util.cu:428-452).  When the three x-cells of a row are
+// consecutive hashes their particles form one contiguous sorted range, which
+// is walked as one loop.  f(q) returns false to stop the walk.
+template <class F>
+__device__ __forceinline__ void walk27(const SceneDesc &d, const uint32_t *__restrict__ offsets, uint32_t shift,
+                                       float4 xp, F &&f)
+{
+    const uint32_t gx = (uint32_t)cell_coord(xp.x, d.cw);
+    const uint32_t gy = (uint32_t)cell_coord(xp.y, d.cw);
+    const uint32_t gz = (uint32_t)cell_coord(xp.z, d.cw);
+    const uint32_t *off = offsets + d.c_off;
+    const uint32_t mx = d.gx - 1u;
+    const uint32_t x0c = (gx - 1u) & mx, x2c = (gx + 1u) & mx;
+    const bool contiguous = (x2c == x0c + 2u);
+    for (int dz = -1; dz <= 1; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
+                                 ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
+            if (contiguous) {
+                const uint32_t st = __ldg(off + row + x0c) + shift;
+                const uint32_t en = __ldg(off + row + x2c + 1u) + shift;
+                for (uint32_t q = st; q != en; ++q)
+                    if (!f(q)) return;
+            } else {
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const uint32_t xc = (gx + (uint32_t)dx) & mx;
+                    const uint32_t st = __ldg(off + row + xc) + shift;
+                    const uint32_t en = __ldg(off + row + xc + 1u) + shift;
+                    for (uint32_t q = st; q != en; ++q)
+                        if (!f(q)) return;
+                }
+            }
+        }
+    }
+}
+
+// Per-tile prologue shared by the particle kernels.
+#define TILE_LOOP_BEGIN                                                   \
+    const uint32_t n_tiles_ = a.ctrl->n_tiles;                            \
+    for (uint32_t t_ = blockIdx.x; t_ < n_tiles_; t_ += gridDim.x) {      \
+        const uint32_t s = __ldg(a.tile_scene + t_);                      \
+        const uint32_t local = __ldg(a.tile_start + t_) + threadIdx.x;
+#define TILE_LOOP_END }
+
+// --------------------------------------------------------------- kernels --
+
+// predict (pbf_solve.cpp:16-25 -> multiplyAddCUDA x2, pbf_predict.cu:15-45),
+// calcHash (pbf_neighbor_search_util.cu:20-37), checkDeleteParticle
+// (pbf_delete.cu:9-28; deleted key = ncell, one past the last cell) and the
+// histogram of countingSort (insertAndCountCUDA, pbf_counting_sort.cu:21-32).
+__global__ void __launch_bounds__(512) k_predict_hash(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const SceneDesc d = a.scenes[s];
+    const uint32_t i = d.p_off + local;
+    const float4 xv = a.x[i];
+    const float4 vv = a.v[i];
+    const float dt = d.dt;
+    float4 ps;
+    ps.x = __fmaf_rn(__fmaf_rn(d.g[0], dt, vv.x), dt, xv.x);
+    ps.y = __fmaf_rn(__fmaf_rn(d.g[1], dt, vv.y), dt, xv.y);
+    ps.z = __fmaf_rn(__fmaf_rn(d.g[2], dt, vv.z), dt, xv.z);
+    ps.w = 0.f;
+    uint32_t key = hash3((uint32_t)cell_coord(ps.x, d.cw), (uint32_t)cell_coord(ps.y, d.cw),
+                         (uint32_t)cell_coord(ps.z, d.cw), d);
+    if (ps.x < d.amin[0] || d.amax[0] < ps.x || ps.y < d.amin[1] || d.amax[1] < ps.y || ps.z < d.amin[2] ||
+        d.amax[2] < ps.z)
+        key = d.ncell;
+    if (!(isfinite(ps.x) && isfinite(ps.y) && isfinite(ps.z))) atomicOr(a.flags + s, PBF_FLAG_NONFINITE);
+    a.xs[i] = ps;
+    a.key[i] = key;
+    a.slot[i] = atomicAdd(a.count + d.c_off + key, 1u);
+    TILE_LOOP_END
+}
+
+// ---- exclusive scan of the cell counts (reduce, spine, down-sweep) ----
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_scan_reduce(StepArgs a)
+{
+    __shared__ uint32_t ws[kScanWarps];
+    const uint32_t n = a.ctrl->n_cells;
+    const uint32_t ntile = (n + kScanTile - 1) / kScanTile;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const uint32_t base = t * kScanTile + warp * kScanItemsPerWarp;
+        uint32_t sum = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 16; ++j) {
+            const uint32_t idx = base + j * 32 + lane;
+            if (idx < n) sum += a.count[idx];
+        }
+#pragma unroll
+        for (uint32_t o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) ws[warp] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tot = 0;
+            for (uint32_t k = 0; k < kScanWarps; ++k) tot += ws[k];
+            a.bsum[t] = tot;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
+{
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    const uint32_t n = a.ctrl->n_cells;
+    const uint32_t ntile = (n + kScanTile - 1) / kScanTile;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < ntile; base += 1024) {
+        const uint32_t idx = base + threadIdx.x;
+        const uint32_t v = idx < ntile ? a.bsum[idx] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (lane == 31) ws[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t wv = ws[lane];
+            ws[lane] = warp_incl_scan(wv) - wv;
+        }
+        __syncthreads();
+        const uint32_t c = carry;
+        if (idx < ntile) a.bsum[idx] = c + ws[warp] + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + ws[warp] + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.offsets[n] = carry;
+}
+
+__global__ void __launch_bounds__(256) k_scan_down(StepArgs a)
+{
+    __shared__ uint32_t ws[kScanWarps];
+    const uint32_t n = a.ctrl->n_cells;
+    const uint32_t ntile = (n + kScanTile - 1) / kScanTile;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const uint32_t base = t * kScanTile + warp * kScanItemsPerWarp;
+        uint32_t vals[16];
+        uint32_t sum = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 16; ++j) {
+            const uint32_t idx = base + j * 32 + lane;
+            vals[j] = idx < n ? a.count[idx] : 0u;
+            sum += vals[j];
+        }
+        uint32_t wsum = sum;
+#pragma unroll
+        for (uint32_t o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+        if (lane == 0) ws[warp] = wsum;
+        __syncthreads();
+        uint32_t run = a.bsum[t];
+        for (uint32_t k = 0; k < warp; ++k) run += ws[k];
+#pragma unroll
+        for (uint32_t j = 0; j < 16; ++j) {
+            const uint32_t idx = base + j * 32 + lane;
+            const uint32_t inc = warp_incl_scan(vals[j]);
+            if (idx < n) {
+                a.offsets[idx] = run + inc - vals[j];
+                a.count[idx] = 0u;  // ready for the next step's histogram
+            }
+            run += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        __syncthreads();
+    }
+}
+
+// Scatter into the cell buckets in atomic-slot order (sortByCountingCUDA,
+// pbf_counting_sort.cu:120-134).
+__global__ void __launch_bounds__(512) k_scatter(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const SceneDesc d = a.scenes[s];
+    const uint32_t i = d.p_off + local;
+    a.tmp[a.offsets[d.c_off + a.key[i]] + a.slot[i]] = local;
+    TILE_LOOP_END
+}
+
+// Stable rank inside the bucket (count of smaller input indices), then the
+// reorder of predicted and old positions (reorderDataCUDA x2,
+// pbf_neighbor_search_util.cu:143-154).  The result equals a stable sort by
+// cell (cub::DeviceRadixSort::SortPairs order).  Buckets larger than
+// kStableLimit keep the atomic order (PBF_FLAG_UNSTABLE_ORDER is not part of
+// the ABI; such buckets only arise from degenerate inputs or mass deletion).
+constexpr uint32_t kStableLimit = 4096;
+
+__global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const SceneDesc d = a.scenes[s];
+    const uint32_t i = d.p_off + local;
+    const uint32_t gk = d.c_off + a.key[i];
+    const uint32_t st = a.offsets[gk], en = a.offsets[gk + 1];
+    uint32_t rank;
+    if (en - st <= kStableLimit) {
+        rank = 0;
+        for (uint32_t t = st; t < en; ++t) rank += (__ldg(a.tmp + t) < local) ? 1u : 0u;
+    } else {
+        rank = a.slot[i];
+    }
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t g = d.p_off + (st - base) + rank;
+    a.perm[g] = local;
+    a.xa[g] = a.xs[i];
+    a.xold[g] = a.x[i];
+    TILE_LOOP_END
+}
+
+// Neighbour list (detectNeighborsCUDA<uint32_t>, pbf_neighbor_search_util.cu:454-482,
+// cap max_pair-1, self included) fused with the iteration-0 lambda
+// (calcScalingFactorCUDA cached, pbf_constraint.cu:168-209): at iteration 0
+// the working positions are the sorted predicted positions, so the pair
+// terms can be summed while the list is built.
+__global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const uint32_t shift = d.p_off - base;
+    const float4 xp = a.xa[i];
+    const float h2 = d.h2, inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const uint32_t cap = d.cap;
+    const uint64_t stride = a.nbr_stride;
+    uint32_t *nl = a.nbr + i;
+    const float4 *__restrict__ xa = a.xa;
+    uint32_t cnt = 0;
+    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+    walk27(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
+        const float4 xq = __ldg(xa + q);
+        if (dist2_exact(xp, xq) < h2) {
+            nl[(uint64_t)cnt * stride] = q;
+            ++cnt;
+            const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
+            ks += pk.W;
+            g0 += pk.gx;
+            g1 += pk.gy;
+            g2 += pk.gz;
+            kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+        }
+        return cnt < cap;
+    });
+    a.nnb[i] = (uint8_t)cnt;
+    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
+    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    TILE_LOOP_END
+}
+
+// lambda for iterations >= 1 (memorizeKernelCalc + calcScalingFactor,
+// pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
+// per-pair cache: W and grad W are recomputed from positions).
+__global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__restrict__ xc)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const float4 xp = xc[i];
+    const uint32_t nn = a.nnb[i];
+    const uint64_t stride = a.nbr_stride;
+    const uint32_t *nl = a.nbr + i;
+    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+#pragma unroll 4
+    for (uint32_t k = 0; k < nn; ++k) {
+        const uint32_t q = __ldg(nl + (uint64_t)k * stride);
+        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
+        ks += pk.W;
+        g0 += pk.gx;
+        g1 += pk.gy;
+        g2 += pk.gz;
+        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+    }
+    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
+    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    TILE_LOOP_END
+}
+
+// delta-p with s_corr (calcPositionUpdateCUDA cached, pbf_position_update.cu:131-188),
+// boundary response (pbf_response_collision.cu:12-66) and x += dp
+// (updateInterimPositionCUDA, pbf_constraint.cu:335-345), written to a second
+// buffer so neighbours still read the old positions.  On the last iteration
+// the velocity update (updateVelocityCUDA, pbf_update.cu:25-39) is fused in:
+// v = (x_new - x_old) / dt, written with x_new to the particle phase.
+__global__ void __launch_bounds__(512) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
+                                          float4 *__restrict__ vo, int last)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (last && local == 0) a.scene_num[s] = live;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const float4 xp = xc[i];
+    const float li = a.lam[i];
+    const float sci = (li < 0.f) ? -li : 0.f;
+    const int mode = d.tensile_mode;
+    const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
+    const int sn = d.scorr_n;
+    const uint32_t nn = a.nnb[i];
+    const uint64_t stride = a.nbr_stride;
+    const uint32_t *nl = a.nbr + i;
+    const float *__restrict__ lam = a.lam;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll 4
+    for (uint32_t k = 0; k < nn; ++k) {
+        const uint32_t q = __ldg(nl + (uint64_t)k * stride);
+        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
+        const float lj = __ldg(lam + q);
+        float corr = 0.f;
+        if (mode == PBF_TENSILE_REFERENCE) {
+            const float kr2 = pk.W * pk.W;
+            const float tc = 10.f * (kr2 * kr2) * inv_k;
+            corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
+        } else if (mode == PBF_TENSILE_TEXTBOOK) {
+            const float ratio = pk.W * inv_wdq;
+            float pw = 1.f;
+            for (int e = 0; e < sn; ++e) pw *= ratio;
+            corr = sk * pw;
+        }
+        const float c = -(li + lj + corr);
+        s0 += c * pk.gx;
+        s1 += c * pk.gy;
+        s2 += c * pk.gz;
+    }
+    float3 dp = make_float3(s0 * d.m * d.inv_rho0, s1 * d.m * d.inv_rho0, s2 * d.m * d.inv_rho0);
+    const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
+    if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
+    const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
+    xo[i] = xn;
+    if (last) {
+        const float4 xo_ = a.xold[i];
+        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+    }
+    TILE_LOOP_END
+}
+
+// iters == 0: positions stay at the prediction; v from the velocity update.
+__global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict__ vo)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local == 0) a.scene_num[s] = live;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float4 xn = a.xa[i];
+    const float4 xo_ = a.xold[i];
+    a.x[i] = xn;
+    vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+    TILE_LOOP_END
+}
+
+// Vorticity, pass 1 (calcVorticityCUDA, pbf_vorticity_confinement.cu:87-115):
+// omega_i = m/rho0 * sum_j (v_j - v_i) x r_hat * W'(r), uncapped 27-cell walk.
+// Mode REFERENCE passes h where 1/h is expected (pbf_vorticity_confinement.cu:28).
+__global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__restrict__ vs)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    if (d.vort_mode == PBF_VORTICITY_OFF) continue;
+    const uint32_t i = d.p_off + local;
+    const float4 xi = a.x[i], vi = vs[i];
+    const bool ref = d.vort_mode == PBF_VORTICITY_REFERENCE;
+    const float kh = ref ? d.h : d.inv_h;
+    // W'(r) = 0 beyond h for the textbook kernel, so those candidates add
+    // nothing; the reference form (kernel scaled by h, not 1/h) reaches the
+    // whole 27-cell block and is walked in full
+    const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
+    const float4 *__restrict__ x = a.x;
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+        if (r2 > 0.f && r2 <= rcut2) {
+            const float inv_r = rsqrtf(r2);
+            const float4 vj = __ldg(vs + j);
+            const float v0 = vj.x - vi.x, v1 = vj.y - vi.y, v2 = vj.z - vi.z;
+            const float wd = wspiky_d(r2 * inv_r, kh) * inv_r;
+            w0 += (v1 * p2 - v2 * p1) * wd;
+            w1 += (v2 * p0 - v0 * p2) * wd;
+            w2 += (v0 * p1 - v1 * p0) * wd;
+        }
+        return true;
+    });
+    const float mr = d.m * d.inv_rho0;
+    a.w[i] = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
+    TILE_LOOP_END
+}
+
+// Vorticity, pass 2 (addVorticityConfinementCUDA, pbf_vorticity_confinement.cu:192-222).
+__global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restrict__ vs)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    if (d.vort_mode == PBF_VORTICITY_OFF) continue;
+    const uint32_t i = d.p_off + local;
+    const float4 xi = a.x[i];
+    const bool ref = d.vort_mode == PBF_VORTICITY_REFERENCE;
+    const float kh = ref ? d.h : d.inv_h;
+    const float sgn = ref ? 1.f : -1.f;
+    const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
+    const float4 *__restrict__ x = a.x;
+    const float4 *__restrict__ w = a.w;
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+        if (r2 > 0.f && r2 <= rcut2) {
+            const float inv_r = rsqrtf(r2);
+            const float4 wj = __ldg(w + j);
+            const float wl = sqrtf(wj.x * wj.x + wj.y * wj.y + wj.z * wj.z);
+            const float f = sgn * wl * wspiky_d(r2 * inv_r, kh) * inv_r;
+            n0 += f * p0;
+            n1 += f * p1;
+            n2 += f * p2;
+        }
+        return true;
+    });
+    const float4 wi = w[i];
+    const float mr = d.m * d.inv_rho0;
+    float4 v = vs[i];
+    if (ref) {
+        if (sqrtf(n0 * n0 + n1 * n1 + n2 * n2) > 0.f) {
+            n0 = n0 * d.m * d.inv_rho0;
+            n1 = n1 * d.m * d.inv_rho0;
+            n2 = n2 * d.m * d.inv_rho0;
+            const float ln = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+            n0 /= ln; n1 /= ln; n2 /= ln;
+            const float c0 = n1 * wi.z - n2 * wi.y, c1 = n2 * wi.x - n0 * wi.z, c2 = n0 * wi.y - n1 * wi.x;
+            v.x = v.x + d.vort_eps * c0 / d.inv_rho0 * d.dt;
+            v.y = v.y + d.vort_eps * c1 / d.inv_rho0 * d.dt;
+            v.z = v.z + d.vort_eps * c2 / d.inv_rho0 * d.dt;
+        }
+    } else {
+        n0 *= mr; n1 *= mr; n2 *= mr;
+        const float ln = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+        if (ln > 0.f) {
+            n0 /= ln; n1 /= ln; n2 /= ln;
+            const float c0 = n1 * wi.z - n2 * wi.y, c1 = n2 * wi.x - n0 * wi.z, c2 = n0 * wi.y - n1 * wi.x;
+            v.x = v.x + d.dt * d.vort_eps * c0;
+            v.y = v.y + d.dt * d.vort_eps * c1;
+            v.z = v.z + d.dt * d.vort_eps * c2;
+        }
+    }
+    vs[i] = v;
+    TILE_LOOP_END
+}
+
+// XSPH (calcXSPHCUDA, pbf_xsph.cu:84-113): v_i += c m/rho0 sum_j (v_j - v_i) W(r_ij),
+// uncapped 27-cell walk, NaN guard.
+__global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restrict__ vs, float4 *__restrict__ vo)
+{
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float4 xi = a.x[i], vi = vs[i];
+    if (d.xsph_mode == 0) {  // scene without XSPH in a batch that has some
+        vo[i] = vi;
+        continue;
+    }
+    const float inv_h = d.inv_h, alpha6 = d.alpha6;
+    // W = 0 beyond h: those candidates add nothing (a non-finite velocity of
+    // a non-neighbour is no longer folded into the sum; such particles raise
+    // PBF_FLAG_NONFINITE in the next step's prediction)
+    const float rcut2 = d.h2 * 1.0001f;
+    const float4 *__restrict__ x = a.x;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+        if (r2 <= rcut2) {
+            const float W = wpoly6(sqrtf(r2), inv_h, alpha6);
+            const float4 vj = __ldg(vs + j);
+            s0 += (vj.x - vi.x) * W;
+            s1 += (vj.y - vi.y) * W;
+            s2 += (vj.z - vi.z) * W;
+        }
+        return true;
+    });
+    float4 out = vi;
+    if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
+        const float c = d.xsph_c * d.m * d.inv_rho0;
+        out.x = vi.x + c * s0;
+        out.y = vi.y + c * s1;
+        out.z = vi.z + c * s2;
+    }
+    vo[i] = out;
+    TILE_LOOP_END
+}
+
+__global__ void __launch_bounds__(512) k_unpack(StepArgs a, const uint32_t *__restrict__ pack_off,
+                                                const float *__restrict__ sx, const float *__restrict__ sv)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const uint64_t q = (uint64_t)pack_off[s] + local;
+    const uint32_t i = a.scenes[s].p_off + local;
+    a.x[i] = make_float4(sx[3 * q], sx[3 * q + 1], sx[3 * q + 2], 0.f);
+    a.v[i] = sv ? make_float4(sv[3 * q], sv[3 * q + 1], sv[3 * q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    TILE_LOOP_END
+}
+
+__global__ void __launch_bounds__(512) k_pack(StepArgs a, const uint32_t *__restrict__ pack_off,
+                                              float *__restrict__ dx, float *__restrict__ dv)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const uint64_t q = (uint64_t)pack_off[s] + local;
+    const uint32_t i = a.scenes[s].p_off + local;
+    if (dx) {
+        const float4 t = a.x[i];
+        dx[3 * q] = t.x;
+        dx[3 * q + 1] = t.y;
+        dx[3 * q + 2] = t.z;
+    }
+    if (dv) {
+        const float4 t = a.v[i];
+        dv[3 * q] = t.x;
+        dv[3 * q + 1] = t.y;
+        dv[3 * q + 2] = t.z;
+    }
+    TILE_LOOP_END
+}
+
+__global__ void k_set_u32(uint32_t *dst, uint32_t value) { *dst = value; }
+
+__global__ void k_aos3_to_f4(const float *__restrict__ src, float4 *__restrict__ dst, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f);
+}
+
+__global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__ dst, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 v = src[i];
+        dst[3 * i] = v.x;
+        dst[3 * i + 1] = v.y;
+        dst[3 * i + 2] = v.z;
+    }
+}
+
+}  // namespace
+
+// Resident blocks per SM for the heaviest tile kernels at this block size.
+uint32_t blocks_per_sm(uint32_t tile)
+{
+    int a = 0, b = 0, c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp, (int)tile, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_neighbors_lambda, (int)tile, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda, (int)tile, 0);
+    int m = a < b ? a : b;
+    m = m < c ? m : c;
+    return m > 0 ? (uint32_t)m : 1u;
+}
+
+void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st)
+{
+    if (n) k_aos3_to_f4<<<(n + 255) / 256, 256, 0, st>>>(src, dst, n);
+}
+
+void launch_f4_to_aos3(const float4 *src, float *dst, uint32_t n, cudaStream_t st)
+{
+    if (n) k_f4_to_aos3<<<(n + 255) / 256, 256, 0, st>>>(src, dst, n);
+}
+
+void launch_set_u32(uint32_t *dst, uint32_t value, cudaStream_t st) { k_set_u32<<<1, 1, 0, st>>>(dst, value); }
+
+void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, const float *src_x,
+                   const float *src_v, cudaStream_t st)
+{
+    k_unpack<<<sh.grid, sh.tile, 0, st>>>(a, pack_off, src_x, src_v);
+}
+
+void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, float *dst_x, float *dst_v,
+                 cudaStream_t st)
+{
+    k_pack<<<sh.grid, sh.tile, 0, st>>>(a, pack_off, dst_x, dst_v);
+}
+
+uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool xsph, bool vort,
+                      cudaStream_t st, StepHook *hook)
+{
+    uint32_t nl = 0;
+    const dim3 g(sh.grid), b(sh.tile);
+#define PBF_LAUNCHED(name)                \
+    do {                                  \
+        ++nl;                             \
+        if (hook) hook->launched(name);   \
+    } while (0)
+    k_predict_hash<<<g, b, 0, st>>>(a);
+    PBF_LAUNCHED("k_predict_hash");
+    k_scan_reduce<<<sh.scan_grid, 256, 0, st>>>(a);
+    PBF_LAUNCHED("k_scan_reduce");
+    k_scan_spine<<<1, 1024, 0, st>>>(a);
+    PBF_LAUNCHED("k_scan_spine");
+    k_scan_down<<<sh.scan_grid, 256, 0, st>>>(a);
+    PBF_LAUNCHED("k_scan_down");
+    k_scatter<<<g, b, 0, st>>>(a);
+    PBF_LAUNCHED("k_scatter");
+    k_rank_reorder<<<g, b, 0, st>>>(a);
+    PBF_LAUNCHED("k_rank_reorder");
+    k_neighbors_lambda<<<g, b, 0, st>>>(a);
+    PBF_LAUNCHED("k_neighbors_lambda");
+    float4 *vfinal = xsph ? a.vt : a.v;
+    float4 *cur = a.xa, *nxt = a.xb;
+    for (int it = 0; it < iters; ++it) {
+        if (it > 0) {
+            k_lambda<<<g, b, 0, st>>>(a, cur);
+            PBF_LAUNCHED("k_lambda");
+        }
+        const bool last = (it == iters - 1);
+        float4 *out = last ? a.x : nxt;
+        k_dp<<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        PBF_LAUNCHED("k_dp");
+        float4 *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    if (iters <= 0) {
+        k_finalize<<<g, b, 0, st>>>(a, vfinal);
+        PBF_LAUNCHED("k_finalize");
+    }
+    if (vort) {
+        k_vort_omega<<<g, b, 0, st>>>(a, vfinal);
+        PBF_LAUNCHED("k_vort_omega");
+        k_vort_apply<<<g, b, 0, st>>>(a, vfinal);
+        PBF_LAUNCHED("k_vort_apply");
+    }
+    if (xsph) {
+        k_xsph<<<g, b, 0, st>>>(a, a.vt, a.v);
+        PBF_LAUNCHED("k_xsph");
+    }
+#undef PBF_LAUNCHED
+    return nl;
+}
+
+}  // namespace pbf103
