@@ -23,7 +23,7 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
+
 import os
 import statistics
 import subprocess
@@ -131,19 +131,8 @@ class ClockSampler:
 def shard_scenes(n_scenes: int, rank: int, world: int):
     """Replicas: every rank runs its own full batched workload with its own
     seeds (weak scaling); no data-path collective."""
-    from ssf_pbf_cuda_gb300 import scenes
-    sc = scenes.config4(n_scenes)
-    if rank == 0:
-        return sc
-    # different seeds per rank, same size distribution
-    import numpy as np
-    rng = scenes.rng_for(4 + 7919 * rank)
-    out = []
-    for s in range(n_scenes):
-        n = int(round(math.exp(rng.uniform(math.log(4096), math.log(65536)))))
-        out.append(scenes._random_scene(rng, 1000 + s + 100000 * rank, n))
-    del np
-    return out
+    from ssf_pbf_cuda_gb300 import replicas
+    return replicas.rank_scenes(n_scenes, rank, world)
 
 
 def cpu_baseline_sample(scs, params_fn, seconds: float = 10.0):

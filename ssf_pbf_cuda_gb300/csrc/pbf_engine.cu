@@ -8,7 +8,7 @@
 
 namespace pbf103 {
 
-uint32_t blocks_per_sm(uint32_t tile);  // pbf_kernels.cu
+uint32_t blocks_per_sm(uint32_t tile, uint32_t chunk);  // pbf_kernels.cu
 void set_last_error(const char *what, cudaError_t e);
 
 #define CK(call)                                      \
@@ -609,7 +609,8 @@ LaunchShape Batch::shape_for(uint32_t tile) const
 {
     LaunchShape sh;
     sh.tile = tile;
-    const uint32_t bps = std::max<uint32_t>(1, blocks_per_sm(tile));
+    sh.chunk = chunk_;
+    const uint32_t bps = std::max<uint32_t>(1, blocks_per_sm(tile, chunk_));
     const uint32_t full = (uint32_t)sms_ * bps;
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
     sh.grid = std::min(full, nt);
@@ -667,6 +668,7 @@ pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
         k.tile = sh.tile;
         k.grid = sh.grid;
         k.scan_grid = sh.scan_grid;
+        k.chunk = sh.chunk;
         if (!exec_ || !(k == key_)) {
             if (exec_) {
                 cudaGraphExecDestroy(exec_);
@@ -912,6 +914,13 @@ pbf_status Batch::set_tile(uint32_t tile)
     return PBF_SUCCESS;
 }
 
+pbf_status Batch::set_chunk(uint32_t chunk)
+{
+    if (chunk != 4 && chunk != 8) return PBF_ERROR_INVALID_ARGUMENT;
+    chunk_ = chunk;
+    return PBF_SUCCESS;
+}
+
 pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
 {
     CK(cudaSetDevice(device_));
@@ -945,11 +954,13 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     const uint32_t cands[] = {128, 256, 512, 64};
-    uint32_t best = tile_;
+    const uint32_t chunks[] = {8, 4};
+    uint32_t best = tile_, best_chunk = chunk_;
     float best_ms = 1e30f;
-    const uint32_t orig = tile_;
-    for (uint32_t t : cands) {
+    for (uint32_t t : cands)
+    for (uint32_t ch : chunks) {
         set_tile(t);
+        chunk_ = ch;
         rc = upload(st);
         if (rc != PBF_SUCCESS) break;
         run(iters, st, false);  // warm-up
@@ -962,11 +973,12 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
         if (ms < best_ms) {
             best_ms = ms;
             best = t;
+            best_chunk = ch;
         }
         CK(restore());
     }
-    (void)orig;
     set_tile(best);
+    chunk_ = best_chunk;
     rc = upload(st);
     CK(cudaStreamSynchronize(st));
     cudaEventDestroy(e0);

@@ -83,6 +83,9 @@ public:
     // one step without a graph, with events between kernels
     pbf_status profile_step(int iters, cudaStream_t st, float *ms, char *names, uint32_t max, uint32_t *n);
     pbf_status set_tile(uint32_t tile);
+    pbf_status set_chunk(uint32_t chunk);
+    uint32_t tile() const { return tile_; }
+    uint32_t chunk() const { return chunk_; }
     void set_graph_mode(bool on) { graph_mode_ = on; }
     uint32_t last_launches() const { return last_launches_; }
     uint32_t num_scenes() const;
@@ -134,17 +137,18 @@ private:
 
     // launch configuration and graph cache
     uint32_t tile_ = 256;
+    uint32_t chunk_ = 8;
     bool graph_mode_ = true;
     cudaStream_t cap_stream_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     struct GraphKey {
         int iters = -1;
         bool xsph = false, vort = false;
-        uint32_t tile = 0, grid = 0, scan_grid = 0;
+        uint32_t tile = 0, grid = 0, scan_grid = 0, chunk = 0;
         bool operator==(const GraphKey &o) const
         {
             return iters == o.iters && xsph == o.xsph && vort == o.vort && tile == o.tile && grid == o.grid &&
-                   scan_grid == o.scan_grid;
+                   scan_grid == o.scan_grid && chunk == o.chunk;
         }
     } key_;
     uint32_t last_launches_ = 0;

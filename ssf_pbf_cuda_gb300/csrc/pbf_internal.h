@@ -86,6 +86,7 @@ struct LaunchShape {
     uint32_t tile;        // particles per tile = threads per block
     uint32_t grid;        // persistent grid (blocks) for tile kernels
     uint32_t scan_grid;   // grid for the scan kernels
+    uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
 };
 
 // Called after every kernel launch of a step (per-kernel event timing).

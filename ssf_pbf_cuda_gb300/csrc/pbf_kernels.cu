@@ -219,6 +219,41 @@ __device__ __forceinline__ void walk27(const SceneDesc &d, const uint32_t *__res
     }
 }
 
+// walk27 with the per-neighbour work taken out of the walk: candidates that
+// pass accept(j) are queued in a small per-thread buffer and handed to use(j)
+// in batches, so the neighbour math is not executed masked for every
+// candidate of the walk.  use() sees the accepted candidates in walk order.
+template <class A, class U>
+__device__ __forceinline__ void walk27_batched(const SceneDesc &d, const uint32_t *__restrict__ offsets,
+                                               uint32_t shift, float4 xp, A &&accept, U &&use)
+{
+    constexpr int kBuf = 32;
+    uint32_t buf[kBuf];
+    int nb = 0;
+    walk27(d, offsets, shift, xp, [&](uint32_t j) -> bool {
+        if (accept(j)) {
+            buf[nb++] = j;
+            if (nb == kBuf) {
+                for (int k = 0; k < kBuf; ++k) use(buf[k]);
+                nb = 0;
+            }
+        }
+        return true;
+    });
+    for (int k = 0; k < nb; ++k) use(buf[k]);
+}
+
+// Request list slots [k0, k0 + kChunk) of one particle (slot-major layout);
+// slots past nn read nothing.  kChunk (neighbours per chunk in the lambda /
+// delta-p passes) trades registers for loads in flight; the autotuner picks it.
+template <int kChunk>
+__device__ __forceinline__ void prefetch_idx(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t k0,
+                                             uint32_t nn, uint32_t (&q)[kChunk])
+{
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) q[c] = (k0 + c < nn) ? __ldg(nl + (uint64_t)(k0 + c) * stride) : 0u;
+}
+
 // Per-tile prologue shared by the particle kernels.
 #define TILE_LOOP_BEGIN                                                   \
     const uint32_t n_tiles_ = a.ctrl->n_tiles;                            \
@@ -430,23 +465,30 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
     const uint64_t stride = a.nbr_stride;
     uint32_t *nl = a.nbr + i;
     const float4 *__restrict__ xa = a.xa;
+    // phase 1: the walk only tests and records (lanes of a warp accept
+    // different candidates, so pair math inside the walk would run masked
+    // for almost every candidate)
     uint32_t cnt = 0;
-    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
     walk27(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
-        const float4 xq = __ldg(xa + q);
-        if (dist2_exact(xp, xq) < h2) {
+        if (dist2_exact(xp, __ldg(xa + q)) < h2) {
             nl[(uint64_t)cnt * stride] = q;
             ++cnt;
-            const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
-            ks += pk.W;
-            g0 += pk.gx;
-            g1 += pk.gy;
-            g2 += pk.gz;
-            kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
         }
         return cnt < cap;
     });
     a.nnb[i] = (uint8_t)cnt;
+    // phase 2: lambda over the list just written (L2-resident)
+    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+#pragma unroll 4
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t q = nl[(uint64_t)k * stride];
+        const PairK pk = pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta);
+        ks += pk.W;
+        g0 += pk.gx;
+        g1 += pk.gy;
+        g2 += pk.gz;
+        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+    }
     const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
     const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
     a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
@@ -456,6 +498,7 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
 // lambda for iterations >= 1 (memorizeKernelCalc + calcScalingFactor,
 // pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
 // per-pair cache: W and grad W are recomputed from positions).
+template <int kChunk>
 __global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__restrict__ xc)
 {
     TILE_LOOP_BEGIN
@@ -470,15 +513,29 @@ __global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__rest
     const uint64_t stride = a.nbr_stride;
     const uint32_t *nl = a.nbr + i;
     float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-#pragma unroll 4
-    for (uint32_t k = 0; k < nn; ++k) {
-        const uint32_t q = __ldg(nl + (uint64_t)k * stride);
-        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
-        ks += pk.W;
-        g0 += pk.gx;
-        g1 += pk.gy;
-        g2 += pk.gz;
-        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+    // chunks of kChunk neighbours: the next chunk's indices are requested
+    // before this chunk's positions, so index and position latencies overlap
+    uint32_t qn[kChunk];
+    prefetch_idx(nl, stride, 0, nn, qn);
+    for (uint32_t k0 = 0; k0 < nn; k0 += kChunk) {
+        uint32_t q[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
+        prefetch_idx(nl, stride, k0 + kChunk, nn, qn);
+        float4 xq[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) xq[c] = (k0 + c < nn) ? __ldg(xc + q[c]) : xp;
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) {
+            if (k0 + c < nn) {
+                const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
+                ks += pk.W;
+                g0 += pk.gx;
+                g1 += pk.gy;
+                g2 += pk.gz;
+                kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+            }
+        }
     }
     const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
     const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
@@ -492,6 +549,7 @@ __global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__rest
 // buffer so neighbours still read the old positions.  On the last iteration
 // the velocity update (updateVelocityCUDA, pbf_update.cu:25-39) is fused in:
 // v = (x_new - x_old) / dt, written with x_new to the particle phase.
+template <int kChunk>
 __global__ void __launch_bounds__(512) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
                                           float4 *__restrict__ vo, int last)
 {
@@ -514,26 +572,43 @@ __global__ void __launch_bounds__(512) k_dp(StepArgs a, const float4 *__restrict
     const uint32_t *nl = a.nbr + i;
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-#pragma unroll 4
-    for (uint32_t k = 0; k < nn; ++k) {
-        const uint32_t q = __ldg(nl + (uint64_t)k * stride);
-        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
-        const float lj = __ldg(lam + q);
-        float corr = 0.f;
-        if (mode == PBF_TENSILE_REFERENCE) {
-            const float kr2 = pk.W * pk.W;
-            const float tc = 10.f * (kr2 * kr2) * inv_k;
-            corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
-        } else if (mode == PBF_TENSILE_TEXTBOOK) {
-            const float ratio = pk.W * inv_wdq;
-            float pw = 1.f;
-            for (int e = 0; e < sn; ++e) pw *= ratio;
-            corr = sk * pw;
+    uint32_t qn[kChunk];
+    prefetch_idx(nl, stride, 0, nn, qn);
+    for (uint32_t k0 = 0; k0 < nn; k0 += kChunk) {
+        uint32_t q[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
+        prefetch_idx(nl, stride, k0 + kChunk, nn, qn);
+        float4 xq[kChunk];
+        float lq[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) {
+            const bool ok = k0 + c < nn;
+            xq[c] = ok ? __ldg(xc + q[c]) : xp;
+            lq[c] = ok ? __ldg(lam + q[c]) : 0.f;
         }
-        const float c = -(li + lj + corr);
-        s0 += c * pk.gx;
-        s1 += c * pk.gy;
-        s2 += c * pk.gz;
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) {
+            if (k0 + c < nn) {
+                const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
+                const float lj = lq[c];
+                float corr = 0.f;
+                if (mode == PBF_TENSILE_REFERENCE) {
+                    const float kr2 = pk.W * pk.W;
+                    const float tc = 10.f * (kr2 * kr2) * inv_k;
+                    corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
+                } else if (mode == PBF_TENSILE_TEXTBOOK) {
+                    const float ratio = pk.W * inv_wdq;
+                    float pw = 1.f;
+                    for (int e = 0; e < sn; ++e) pw *= ratio;
+                    corr = sk * pw;
+                }
+                const float cc = -(li + lj + corr);
+                s0 += cc * pk.gx;
+                s1 += cc * pk.gy;
+                s2 += cc * pk.gz;
+            }
+        }
     }
     float3 dp = make_float3(s0 * d.m * d.inv_rho0, s1 * d.m * d.inv_rho0, s2 * d.m * d.inv_rho0);
     const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
@@ -585,11 +660,18 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
     const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
     const float4 *__restrict__ x = a.x;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
-    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
-        const float4 xj = __ldg(x + j);
-        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-        if (r2 > 0.f && r2 <= rcut2) {
+    walk27_batched(
+        d, a.offsets, d.p_off - base, xi,
+        [&](uint32_t j) -> bool {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+            return r2 > 0.f && r2 <= rcut2;
+        },
+        [&](uint32_t j) {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
             const float inv_r = rsqrtf(r2);
             const float4 vj = __ldg(vs + j);
             const float v0 = vj.x - vi.x, v1 = vj.y - vi.y, v2 = vj.z - vi.z;
@@ -597,9 +679,7 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             w0 += (v1 * p2 - v2 * p1) * wd;
             w1 += (v2 * p0 - v0 * p2) * wd;
             w2 += (v0 * p1 - v1 * p0) * wd;
-        }
-        return true;
-    });
+        });
     const float mr = d.m * d.inv_rho0;
     a.w[i] = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
     TILE_LOOP_END
@@ -623,11 +703,18 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
     const float4 *__restrict__ x = a.x;
     const float4 *__restrict__ w = a.w;
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
-        const float4 xj = __ldg(x + j);
-        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-        if (r2 > 0.f && r2 <= rcut2) {
+    walk27_batched(
+        d, a.offsets, d.p_off - base, xi,
+        [&](uint32_t j) -> bool {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+            return r2 > 0.f && r2 <= rcut2;
+        },
+        [&](uint32_t j) {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
             const float inv_r = rsqrtf(r2);
             const float4 wj = __ldg(w + j);
             const float wl = sqrtf(wj.x * wj.x + wj.y * wj.y + wj.z * wj.z);
@@ -635,9 +722,7 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             n0 += f * p0;
             n1 += f * p1;
             n2 += f * p2;
-        }
-        return true;
-    });
+        });
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
     float4 v = vs[i];
@@ -690,19 +775,22 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
     const float rcut2 = d.h2 * 1.0001f;
     const float4 *__restrict__ x = a.x;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    walk27(d, a.offsets, d.p_off - base, xi, [&](uint32_t j) -> bool {
-        const float4 xj = __ldg(x + j);
-        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-        if (r2 <= rcut2) {
-            const float W = wpoly6(sqrtf(r2), inv_h, alpha6);
+    walk27_batched(
+        d, a.offsets, d.p_off - base, xi,
+        [&](uint32_t j) -> bool {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            return p0 * p0 + p1 * p1 + p2 * p2 <= rcut2;
+        },
+        [&](uint32_t j) {
+            const float4 xj = __ldg(x + j);
+            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+            const float W = wpoly6(sqrtf(p0 * p0 + p1 * p1 + p2 * p2), inv_h, alpha6);
             const float4 vj = __ldg(vs + j);
             s0 += (vj.x - vi.x) * W;
             s1 += (vj.y - vi.y) * W;
             s2 += (vj.z - vi.z) * W;
-        }
-        return true;
-    });
+        });
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
         const float c = d.xsph_c * d.m * d.inv_rho0;
@@ -772,12 +860,17 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 }  // namespace
 
 // Resident blocks per SM for the heaviest tile kernels at this block size.
-uint32_t blocks_per_sm(uint32_t tile)
+uint32_t blocks_per_sm(uint32_t tile, uint32_t chunk)
 {
     int a = 0, b = 0, c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp, (int)tile, 0);
+    if (chunk == 4) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp<4>, (int)tile, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda<4>, (int)tile, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp<8>, (int)tile, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda<8>, (int)tile, 0);
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_neighbors_lambda, (int)tile, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda, (int)tile, 0);
     int m = a < b ? a : b;
     m = m < c ? m : c;
     return m > 0 ? (uint32_t)m : 1u;
@@ -835,12 +928,14 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            k_lambda<<<g, b, 0, st>>>(a, cur);
+            if (sh.chunk == 4) k_lambda<4><<<g, b, 0, st>>>(a, cur);
+            else k_lambda<8><<<g, b, 0, st>>>(a, cur);
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        k_dp<<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        if (sh.chunk == 4) k_dp<4><<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        else k_dp<8><<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;

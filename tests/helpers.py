@@ -2,6 +2,8 @@
 CPU oracle, and compare them."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from ssf_pbf_cuda_gb300 import api, scenes
@@ -111,3 +113,97 @@ def assert_integer_parity(g: dict, r: dict, params: dict):
         assert a.shape == b.shape, (k, a.shape, b.shape)
         bad = np.nonzero(a != b)[0]
         assert bad.size == 0, f"{k}: {bad.size} mismatches, first at {bad[:5]}: gpu {a[bad[:5]]} oracle {b[bad[:5]]}"
+
+
+# ---------------------------------------------------------------- golden --
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_PARAM_ORDER = ["stable_density", "stable_distance", "particle_mass", "smoothing_length", "time_step",
+                      "relaxation", "xsph_parameter", "vc_parameter"]
+
+
+def golden_files():
+    import glob
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def golden_case(path):
+    """(scene, params, boundary mode arrays, iters, fixture) from a fixture file."""
+    fx = dict(np.load(path))
+    p = api.default_params()
+    for k, val in zip(GOLDEN_PARAM_ORDER, fx["params"]):
+        p[k] = float(val)
+    p["body_force"] = [float(t) for t in fx["body_force"]]
+    p["cell_width"] = p["smoothing_length"]
+    p["grid_size"] = [int(t) for t in fx["ieee_grid"]]
+    sc = scenes.Scene(fx["x_in"], fx["v_in"], tuple(float(t) for t in fx["domain_end"]),
+                      (tuple(float(t) for t in fx["area_min"]), tuple(float(t) for t in fx["area_max"])),
+                      (fx["plane_pts"], fx["plane_nrm"]))
+    return sc, p, int(fx["iters"]), fx
+
+
+def golden_oracle_boundary(O, fx):
+    if not int(fx["use_boundary"]):
+        return None
+    return O.Boundary(inner=fx["inner"], outer=fx["outer"], plane_pts=fx["plane_pts"], plane_nrm=fx["plane_nrm"])
+
+
+def golden_gpu_boundary(fx):
+    if not int(fx["use_boundary"]):
+        return None
+    return api.Boundary(inner_spheres=fx["inner"], outer_spheres=fx["outer"], points_on_planes=fx["plane_pts"],
+                        normals_on_planes=fx["plane_nrm"])
+
+
+def reference_of(fx, variant="ieee"):
+    return {k[len(variant) + 1:]: fx[k] for k in fx if k.startswith(variant + "_")}
+
+
+def compare_to_reference(ours: dict, ref: dict, C: int) -> dict:
+    """Compare a step's outputs with the reference's.  The reference's sort is
+    a counting sort with atomic ranks, so the order inside a cell is
+    arbitrary: integers are compared on sort-invariant forms (sorted hashes,
+    cell ranges, per-cell index sets, neighbour sets by particle id), and
+    positions/velocities by particle id.  ``ours`` holds num, x, v (sorted),
+    perm (sorted -> input), sorted_hash, cell_start, cell_end and
+    neighbor_list (reference layout)."""
+    rep = {}
+    num = int(ref["num"])
+    assert ours["num"] == num, (ours["num"], num)
+    # sorted hashes of live particles; deleted ones carry C here, Gz*Gy*Gz-1 there
+    assert np.array_equal(np.asarray(ours["sorted_hash"])[:num], ref["sorted_hash"][:num])
+    cs_r, ce_r = ref["cell_start"], ref["cell_end"]
+    ne = cs_r != 0xFFFFFFFF
+    assert np.array_equal(ne, ours["cell_start"] != 0xFFFFFFFF)
+    assert np.array_equal(ours["cell_start"][ne], cs_r[ne]) and np.array_equal(ours["cell_end"][ne], ce_r[ne])
+    pr = ref["sorted_index"].astype(np.int64)
+    po = np.asarray(ours["perm"]).astype(np.int64)
+    for c in np.nonzero(ne)[0]:
+        s, e = cs_r[c], ce_r[c]
+        assert np.array_equal(np.sort(pr[s:e]), np.sort(po[s:e])), c
+    assert np.array_equal(np.sort(pr[num:]), np.sort(po[num:]))
+    # positions / velocities by particle id
+    xr = np.zeros((len(pr), 3)); xo = np.zeros((len(pr), 3))
+    vr = np.zeros((len(pr), 3)); vo = np.zeros((len(pr), 3))
+    xr[pr[:num]] = ref["x"]; xo[po[:num]] = ours["x"]
+    vr[pr[:num]] = ref["v"]; vo[po[:num]] = ours["v"]
+    rep["pos_rel_err"] = pos_rel_err(xo, xr)
+    rep["vel_abs_err"] = float(np.abs(vo - vr).max(initial=0))
+    # neighbour sets by particle id
+    mp = int(ref["max_pair"])
+
+    def sets(nl, perm):
+        out = {}
+        for p in range(num):
+            base = (p & 31) + ((p >> 5) << 5) * mp
+            ids = []
+            for k in range(mp):
+                q = nl[(k << 5) + base]
+                if q == 0xFFFFFFFF:
+                    break
+                ids.append(int(perm[q]))
+            out[int(perm[p])] = sorted(ids)
+        return out
+
+    so, sr = sets(np.asarray(ours["neighbor_list"]), po), sets(ref["neighbor_list"], pr)
+    rep["neighbor_set_mismatches"] = sum(1 for k in sr if sr[k] != so.get(k))
+    return rep

@@ -1,0 +1,232 @@
+"""Batched engine and continuous-batching server on the GPU.
+
+Each scene's result in a batch must equal (bitwise) the same scene stepped
+alone through the plain single-scene path, and match the oracle within the
+parity tolerance."""
+import numpy as np
+import pytest
+
+import ssf_pbf_cuda_gb300 as pbf
+from ssf_pbf_cuda_gb300 import api, scenes
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_scenes():
+    """Scenes of uneven sizes and different physics modes."""
+    out = []
+    s = 0.05
+    out.append((H.reflike_dam(10, scene_id=31), H.reflike_params()))
+    sc = scenes.dam_break(14, 9, 11, (2.0, 1.5, 1.5), scene_id=32)
+    out.append((sc, api.config_params(scorr_k=1e-4)))
+    sc = scenes.dam_break(7, 20, 6, (1.0, 2.0, 1.0), scene_id=33)
+    out.append((sc, api.config_params(scorr_k=1e-4, vorticity_mode=pbf.PBF_VORTICITY_REFERENCE, xsph_mode=0)))
+    sc = scenes.dam_break(16, 16, 16, (3.0, 2.0, 2.0), scene_id=34, h=1.4 * s, spacing=s)
+    out.append((sc, H.reflike_params()))
+    sc = scenes.dam_break(5, 5, 5, (1.0, 1.0, 1.0), scene_id=35)
+    out.append((sc, api.config_params(tensile_mode=pbf.PBF_TENSILE_OFF, xsph_mode=1, vorticity_mode=0)))
+    return out
+
+
+def make_batch(items, extra_particles=0):
+    n = sum(sc.n for sc, _ in items) + extra_particles
+    cells = sum(int(np.prod(H.resolved(p, sc)["grid_size"])) + 1 for sc, p in items) + 100000
+    b = api.Batch(len(items) + 4, n + 1000, cells, 30)
+    ids = []
+    for sc, p in items:
+        ids.append(b.add_scene(H.resolved(p, sc), sc.n, sc.domain_end, H.gpu_boundary(sc, "planes"), sc.area,
+                               sc.x, sc.v))
+    return b, ids
+
+
+def alone(sc, p, steps):
+    return H.run_gpu(sc, p, "planes", 4, steps=steps, debug=False)
+
+
+def test_alone_equals_in_mix_bitwise(gpu):
+    items = mixed_scenes()
+    b, ids = make_batch(items)
+    for _ in range(2):
+        b.step(4)
+    for (sc, p), sid in zip(items, ids):
+        x, v = b.get_scene(sid)
+        a = alone(sc, p, 2)
+        assert np.array_equal(x, a["x"]) and np.array_equal(v, a["v"])
+
+
+def test_batch_matches_oracle_per_scene(oracle, gpu):
+    items = mixed_scenes()
+    b, ids = make_batch(items)
+    b.step(4)
+    for (sc, p), sid in zip(items, ids):
+        x, v = b.get_scene(sid)
+        r = H.run_oracle(oracle, sc, p, "planes", 4, f64=True)
+        assert H.pos_rel_err(x, r["x"]) <= H.POS_RTOL
+        assert np.abs(v - r["v"]).max(initial=0) <= H.vel_abs_tol(p["time_step"], r["x"])
+
+
+@pytest.mark.parametrize("tile", [64, 128, 256, 512])
+def test_tile_sizes_give_identical_results(gpu, tile):
+    items = mixed_scenes()[:3]
+    b, ids = make_batch(items)
+    b.set_tile(tile)
+    b.step(4)
+    for (sc, p), sid in zip(items, ids):
+        x, _ = b.get_scene(sid)
+        assert np.array_equal(x, alone(sc, p, 1)["x"])
+
+
+def test_remove_and_reuse_slots(gpu):
+    items = mixed_scenes()
+    b, ids = make_batch(items)
+    b.step(4)
+    b.remove_scene(ids[1])
+    b.remove_scene(ids[3])
+    assert b.num_scenes == 3
+    sc, p = items[1]
+    nid = b.add_scene(H.resolved(p, sc), sc.n, sc.domain_end, H.gpu_boundary(sc, "planes"), sc.area, sc.x, sc.v)
+    assert nid in (ids[1], ids[3])
+    b.step(4)
+    x, _ = b.get_scene(nid)
+    assert np.array_equal(x, alone(sc, p, 1)["x"])
+    x0, _ = b.get_scene(ids[0])
+    assert np.array_equal(x0, alone(*items[0], 2)["x"])
+
+
+def test_set_all_get_all_roundtrip(gpu):
+    import torch
+    items = mixed_scenes()
+    b, ids = make_batch(items)
+    assert b.scene_ids() == sorted(ids)
+    counts, x, v = b.get_all()
+    assert list(counts) == [sc.n for sc, _ in items]
+    assert np.array_equal(x, np.concatenate([sc.x for sc, _ in items]))
+    # device round trip with a perturbed state
+    xd = torch.from_numpy(x + 0.001).cuda()
+    vd = torch.from_numpy(v + 0.5).cuda()
+    b.set_all(xd, vd, counts)
+    c2, x2, v2 = b.get_all()
+    assert np.array_equal(x2, x + np.float32(0.001)) and np.array_equal(v2, v + np.float32(0.5))
+
+
+def test_autotune_preserves_state(gpu):
+    items = mixed_scenes()
+    b, ids = make_batch(items)
+    tile = b.autotune(4)
+    assert tile in (64, 128, 256, 512)
+    b.step(4)
+    for (sc, p), sid in zip(items, ids):
+        x, _ = b.get_scene(sid)
+        assert np.array_equal(x, alone(sc, p, 1)["x"])
+
+
+def test_nonfinite_scene_is_isolated(gpu):
+    items = mixed_scenes()[:3]
+    sc, p = items[1]
+    bad = scenes.Scene(sc.x.copy(), sc.v.copy(), sc.domain_end, sc.area, sc.planes)
+    bad.x[5] = np.nan
+    items[1] = (bad, p)
+    b, ids = make_batch(items)
+    b.step(4)
+    assert b.flags(ids[1]) & pbf.PBF_FLAG_NONFINITE
+    assert b.flags(ids[0]) == 0 and b.flags(ids[2]) == 0
+    x0, _ = b.get_scene(ids[0])
+    assert np.array_equal(x0, alone(*items[0], 1)["x"])
+
+
+def test_graph_off_matches_graph_on(gpu):
+    items = mixed_scenes()
+    b1, ids1 = make_batch(items)
+    b2, ids2 = make_batch(items)
+    b2.set_graph_mode(False)
+    for _ in range(3):
+        b1.step(4)
+        b2.step(4)
+    for i1, i2 in zip(ids1, ids2):
+        assert np.array_equal(b1.get_scene(i1)[0], b2.get_scene(i2)[0])
+
+
+def test_profile_step_names_every_kernel(gpu):
+    items = mixed_scenes()
+    b, _ = make_batch(items)
+    prof = b.profile_step(4)
+    names = [n for n, _ in prof]
+    assert names[:7] == ["k_predict_hash", "k_scan_reduce", "k_scan_spine", "k_scan_down", "k_scatter",
+                         "k_rank_reorder", "k_neighbors_lambda"]
+    assert names.count("k_dp") == 4 and names.count("k_lambda") == 3
+    assert b.launches == len(prof)
+
+
+# ------------------------------------------------------------------ server --
+
+def server_requests(n=6):
+    reqs = []
+    for k in range(n):
+        sc = scenes.dam_break(6 + k, 8, 7, (1.5, 1.5, 1.5), scene_id=200 + k)
+        reqs.append((sc, api.config_params(scorr_k=1e-4), 2 + (k % 3)))
+    return reqs
+
+
+def submit_all(srv, reqs):
+    rids = []
+    for sc, p, hz in reqs:
+        rids.append(srv.submit(H.resolved(p, sc), sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz,
+                               planes=sc.planes))
+    return rids
+
+
+def test_server_results_equal_alone(gpu):
+    reqs = server_requests()
+    big = sum(api.scene_bytes(H.resolved(p, sc), sc.n, sc.domain_end) for sc, p, _ in reqs)
+    srv = api.Server(hbm_budget_bytes=big * 2, max_scenes=8, max_particles=20000, max_cells=200000, iters=4)
+    rids = submit_all(srv, reqs)
+    srv.run_until_idle()
+    done = {c["request_id"]: c for c in srv.poll()}
+    assert set(done) == set(rids)
+    for (sc, p, hz), rid in zip(reqs, rids):
+        x, v = srv.result(rid)
+        a = alone(sc, p, hz)
+        assert done[rid]["steps"] == hz
+        assert np.array_equal(x, a["x"]) and np.array_equal(v, a["v"])
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["resident_scenes"] == 0
+
+
+def test_server_budget_admission_queues(gpu):
+    reqs = server_requests(6)
+    per = [api.scene_bytes(H.resolved(p, sc), sc.n, sc.domain_end) for sc, p, _ in reqs]
+    budget = max(per) * 2  # at most two resident at a time
+    srv = api.Server(hbm_budget_bytes=budget, max_scenes=8, max_particles=20000, max_cells=200000, iters=4)
+    rids = submit_all(srv, reqs)
+    srv.run_until_idle()
+    st = srv.stats()
+    assert st["completed"] == 6 and st["peak_resident_bytes"] <= budget
+    comps = srv.poll()
+    assert all(c["admit_s"] >= c["arrival_s"] and c["complete_s"] >= c["admit_s"] for c in comps)
+    for (sc, p, hz), rid in zip(reqs, rids):
+        assert np.array_equal(srv.result(rid)[0], alone(sc, p, hz)["x"])
+
+
+def test_server_rejects_over_budget(gpu):
+    sc, p, hz = server_requests(1)[0]
+    srv = api.Server(hbm_budget_bytes=1000, max_scenes=2, max_particles=5000, max_cells=100000)
+    with pytest.raises(pbf.PbfError) as e:
+        srv.submit(H.resolved(p, sc), sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes)
+    assert e.value.status == 8
+
+
+def test_server_threaded_loop_with_live_arrivals(gpu):
+    import time
+    reqs = server_requests(6)
+    srv = api.Server(hbm_budget_bytes=1 << 32, max_scenes=8, max_particles=20000, max_cells=200000, iters=4)
+    srv.start()
+    rids = []
+    for r in reqs:
+        rids += submit_all(srv, [r])
+        time.sleep(0.002)
+    srv.stop(drain=True)
+    done = {c["request_id"] for c in srv.poll()}
+    assert done == set(rids)
+    for (sc, p, hz), rid in zip(reqs, rids):
+        assert np.array_equal(srv.result(rid)[0], alone(sc, p, hz)["x"])
