@@ -3,9 +3,11 @@
 
 Headline (`value`): the batched workload — 256 independent dam-break scenes,
 4k-64k particles each (log-uniform, seeded), advanced together by the batched
-engine (one CUDA-graph launch sequence per step).  Beside it (`plain`): the
-single large scene, 1,048,576 particles with a 2^21-cell table, through the
-plain single-scene step.  A "step" is one PBF step over the workload's
+engine (one CUDA-graph launch sequence per step).  Beside it, `plain`: the
+same 256 scenes stepped one at a time through the plain single-scene step
+(one pbf_one_step call per scene), and `single_large`: the single large
+scene, 1,048,576 particles with a 2^21-cell table, through the plain step.
+A "step" is one PBF step over the workload's
 synthetic input: each timed step re-loads the seeded initial state from HBM
 (device-to-device, inside the timed region) and runs the full step, so every
 step does identical work.  The configured physics (s_corr k = 0.1 at spacing
@@ -160,6 +162,56 @@ def scene_params(sc):
     return p
 
 
+def run_serving(api, args, device: int) -> dict:
+    """Served stream: Poisson arrivals of dam-break requests (N log-uniform in
+    8k-256k, horizons uniform in 60-600 steps) over `serve_seconds`, admitted
+    by a 150 GB HBM budget into a continuously batched server; returns p50/p99
+    completion latency (arrival -> completion) and served particle-steps/s.
+    Served scenes run chained steps, so they use the configured physics with
+    s_corr k = 1e-4 (k = 0.1 blows up within a few steps at spacing 0.5h)."""
+    import numpy as np
+
+    from ssf_pbf_cuda_gb300 import scenes
+    rate = args.serve_rate
+    n_req = max(1, int(rate * args.serve_seconds))
+    reqs = scenes.config5_requests(n_req, rate)
+    tot_p = sum(sc.n for _, sc, _ in reqs)
+    cells = 0
+    plist = []
+    for _, sc, _ in reqs:
+        p = sc.params(api.config_params(scorr_k=1e-4))
+        p["grid_size"] = list(api.resolve_grid(p, sc.domain_end))
+        plist.append(p)
+        cells += int(np.prod(p["grid_size"])) + 1
+    srv = api.Server(hbm_budget_bytes=150 * 10 ** 9, max_scenes=len(reqs), max_particles=tot_p,
+                     max_cells=cells, iters=ITERS, device=device, tile=args.serve_tile)
+    srv.start()
+    t0 = time.perf_counter()
+    rids = []
+    for (t_arr, sc, hz), p in zip(reqs, plist):
+        wait = t_arr - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        rids.append(srv.submit(p, sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes))
+    srv.stop(drain=True)
+    wall = time.perf_counter() - t0
+    comps = srv.poll(len(reqs) + 16)
+    st = srv.stats()
+    lat = np.array(sorted(c["complete_s"] - c["arrival_s"] for c in comps))
+    qd = np.array(sorted(c["admit_s"] - c["arrival_s"] for c in comps))
+    return {
+        "requests": len(comps), "arrival_rate_hz": rate, "arrival_window_s": args.serve_seconds,
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "p99_queue_s": float(np.percentile(qd, 99)),
+        "particle_steps_per_s": st["particle_steps"] / wall, "busy_particle_steps_per_s":
+            st["particle_steps"] / max(st["busy_s"], 1e-9),
+        "substeps": st["substeps"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9,
+        "hbm_budget_GB": 150, "wall_s": wall,
+        "workload": "dam-break requests, N log-uniform 8k-256k, horizons 60-600 steps, Poisson arrivals, "
+                    "configured physics with s_corr k=1e-4",
+    }
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -215,6 +267,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="arrival window of the serving run (0 = off)")
+    ap.add_argument("--serve-rate", type=float, default=12.0, help="request arrivals per second")
+    ap.add_argument("--serve-tile", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -346,8 +401,37 @@ def main():
                "h2d_bytes_per_step": int(x0h.nbytes + v0h.nbytes), "d2h_bytes_per_step": int(x0h.nbytes + v0h.nbytes),
                "ms_per_step": dt / args.steps * 1e3}
 
-    # ---------------- plain single large scene ----------------
+    # ---------------- plain: the same scenes one at a time ----------------
     plain = None
+    if not args.no_plain and rank == 0:
+        handles = []
+        for k, (sc, p, b) in enumerate(zip(scs, params, bnds)):
+            part = api.PbfParticle(p, sc.n, sc.domain_end, device=local)
+            off = int(counts[:k].sum())
+            handles.append((part, b, sc, x0d[off:off + sc.n], v0d[off:off + sc.n]))
+
+        def plain_scenes_step():
+            for part, b, sc, xd, vd in handles:
+                part.set_particles(xd, vd, stream)
+                api.one_step(part, b, sc.area, ITERS, stream)
+
+        for _ in range(args.warmup):
+            plain_scenes_step()
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for _ in range(args.steps):
+            plain_scenes_step()
+        q1.record(stream)
+        torch.cuda.synchronize()
+        qms = q0.elapsed_time(q1) / args.steps
+        plain = {"value": n_total / (qms / 1e3), "unit": UNIT, "ms_per_step": qms,
+                 "workload": f"the same {len(scs)} scenes, one pbf_one_step call (CUDA graph) per scene",
+                 "batched_over_plain": value / world / (n_total / (qms / 1e3))}
+        del handles
+
+    # ---------------- single large scene ----------------
+    single = None
     if not args.no_plain and rank == 0:
         from ssf_pbf_cuda_gb300 import scenes
         sc = scenes.config2()
@@ -381,11 +465,16 @@ def main():
         pcells = int(np.prod(p["grid_size"])) + 1
         pbp, pbc = ALG_KERNEL.get(ptop, (0, 0))
         pach = (pbp * sc.n + pbc * pcells) / (statistics.mean(pprof[ptop]) / 1e3) / 1e9
-        plain = {"value": sc.n / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
-                 "workload": "plain single scene: 1,048,576 particles (128x128x64 dam break), 2^21-cell table",
-                 "batched_over_plain": value / world / (sc.n / (pms / 1e3)),
-                 "top_kernel": ptop, "top_kernel_GBps": pach, "top_kernel_frac": pach / peak,
-                 "step_alg_GBps": (ALG_STEP_P * sc.n + ALG_STEP_C * pcells) / (pms / 1e3) / 1e9}
+        single = {"value": sc.n / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
+                  "workload": "single scene: 1,048,576 particles (128x128x64 dam break), 2^21-cell table, "
+                              "plain step",
+                  "top_kernel": ptop, "top_kernel_GBps": pach, "top_kernel_frac": pach / peak,
+                  "step_alg_GBps": (ALG_STEP_P * sc.n + ALG_STEP_C * pcells) / (pms / 1e3) / 1e9}
+
+    # ---------------- serving: Poisson arrivals, continuous batching ----------------
+    serving = None
+    if rank == 0 and args.serve_seconds > 0:
+        serving = run_serving(api, args, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -404,7 +493,8 @@ def main():
                        "l2": "inputs larger than L2 (per-step working set >> 129 MB)",
                        "step_definition": "device-resident initial state re-loaded, then one full step",
                        "parallelism": f"replicas x{world}"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
+            "serving": serving,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
         }

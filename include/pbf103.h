@@ -76,8 +76,16 @@ typedef enum pbf_status {
 
 /* vorticity confinement forms */
 #define PBF_VORTICITY_OFF 0       /* as the reference's active step (pbf_solve.cpp:136-138) */
-#define PBF_VORTICITY_REFERENCE 1 /* pbf_vorticity_confinement.cu formulas as written */
-#define PBF_VORTICITY_TEXTBOOK 2
+#define PBF_VORTICITY_REFERENCE 1 /* pbf_vorticity_confinement.cu formulas as written, uncapped
+                                     27-cell walk around the final position */
+#define PBF_VORTICITY_TEXTBOOK 2  /* omega = m/rho0 sum (v_j - v_i) x grad_j W,
+                                     eta = m/rho0 sum |omega_j| grad_i W, v += dt eps (N x omega),
+                                     over the step's neighbour list at the final positions */
+
+/* XSPH forms */
+#define PBF_XSPH_OFF 0            /* as the reference's active step */
+#define PBF_XSPH_WALK 1           /* calcXSPHCUDA: uncapped 27-cell walk (pbf_xsph.cu:51-113) */
+#define PBF_XSPH_LIST 2           /* same sum over the step's neighbour list */
 
 typedef struct pbf_params {
     /* pbf_parameter, src/pbf/pbf_type.h:49-63 */
@@ -98,7 +106,7 @@ typedef struct pbf_params {
     float scorr_k;          /* textbook s_corr k */
     int32_t scorr_n;        /* textbook s_corr n */
     float scorr_dq;         /* textbook s_corr delta-q, in units of h */
-    int32_t xsph_mode;      /* 0 off (reference active step), 1 on */
+    int32_t xsph_mode;      /* PBF_XSPH_* */
     int32_t vorticity_mode; /* PBF_VORTICITY_* */
     uint32_t max_collision_passes; /* bound on the collision projection loop */
     float cell_width;       /* 0 => smoothing_length (pbf_type.cpp:172) */

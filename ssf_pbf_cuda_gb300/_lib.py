@@ -27,6 +27,7 @@ PBF_FLAG_NONFINITE = 0x1
 PBF_FLAG_COLLISION_LIMIT = 0x2
 PBF_TENSILE_REFERENCE, PBF_TENSILE_TEXTBOOK, PBF_TENSILE_OFF = 0, 1, 2
 PBF_VORTICITY_OFF, PBF_VORTICITY_REFERENCE, PBF_VORTICITY_TEXTBOOK = 0, 1, 2
+PBF_XSPH_OFF, PBF_XSPH_WALK, PBF_XSPH_LIST = 0, 1, 2
 
 
 class PbfParams(ctypes.Structure):

@@ -53,9 +53,10 @@ def default_params(**overrides) -> dict:
 
 def config_params(**overrides) -> dict:
     """Physics of the benchmark configs: textbook s_corr (k 0.1, n 4, dq 0.2h),
-    XSPH c 0.01 and textbook vorticity confinement eps 0.0005."""
+    XSPH c 0.01 and textbook vorticity confinement eps 0.0005, both over the
+    step's neighbour list."""
     d = default_params(tensile_mode=L.PBF_TENSILE_TEXTBOOK, scorr_k=0.1, scorr_n=4, scorr_dq=0.2,
-                       xsph_mode=1, xsph_parameter=0.01, vorticity_mode=L.PBF_VORTICITY_TEXTBOOK,
+                       xsph_mode=L.PBF_XSPH_LIST, xsph_parameter=0.01, vorticity_mode=L.PBF_VORTICITY_TEXTBOOK,
                        vc_parameter=0.0005)
     d.update(overrides)
     return d

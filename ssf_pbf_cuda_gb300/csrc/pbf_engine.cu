@@ -105,7 +105,7 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
         return PBF_ERROR_BAD_PARAMETER;
     if (p.max_pair_particle_num < 2 || p.max_pair_particle_num > 256) return PBF_ERROR_INVALID_ARGUMENT;
     if (p.tensile_mode < 0 || p.tensile_mode > 2 || p.vorticity_mode < 0 || p.vorticity_mode > 2 ||
-        p.xsph_mode < 0 || p.xsph_mode > 1 || p.scorr_n < 0 || p.scorr_n > 16 || p.max_collision_passes == 0)
+        p.xsph_mode < 0 || p.xsph_mode > 2 || p.scorr_n < 0 || p.scorr_n > 16 || p.max_collision_passes == 0)
         return PBF_ERROR_INVALID_ARGUMENT;
     const float cw = p.cell_width > 0.f ? p.cell_width : p.smoothing_length;
     uint32_t g[3];

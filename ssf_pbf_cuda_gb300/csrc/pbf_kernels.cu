@@ -254,6 +254,24 @@ __device__ __forceinline__ void prefetch_idx(const uint32_t *__restrict__ nl, ui
     for (int c = 0; c < kChunk; ++c) q[c] = (k0 + c < nn) ? __ldg(nl + (uint64_t)(k0 + c) * stride) : 0u;
 }
 
+// Visit the listed neighbours of one particle in list order, indices
+// prefetched CH at a time.
+template <int CH, class F>
+__device__ __forceinline__ void for_list(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn, F &&f)
+{
+    uint32_t qn[CH];
+    prefetch_idx<CH>(nl, stride, 0, nn, qn);
+    for (uint32_t k0 = 0; k0 < nn; k0 += CH) {
+        uint32_t q[CH];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) q[c] = qn[c];
+        prefetch_idx<CH>(nl, stride, k0 + CH, nn, qn);
+#pragma unroll
+        for (int c = 0; c < CH; ++c)
+            if (k0 + c < nn) f(q[c]);
+    }
+}
+
 // Per-tile prologue shared by the particle kernels.
 #define TILE_LOOP_BEGIN                                                   \
     const uint32_t n_tiles_ = a.ctrl->n_tiles;                            \
@@ -660,18 +678,11 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
     const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
     const float4 *__restrict__ x = a.x;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
-    walk27_batched(
-        d, a.offsets, d.p_off - base, xi,
-        [&](uint32_t j) -> bool {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-            return r2 > 0.f && r2 <= rcut2;
-        },
-        [&](uint32_t j) {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+    auto use = [&](uint32_t j) {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+        if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
             const float4 vj = __ldg(vs + j);
             const float v0 = vj.x - vi.x, v1 = vj.y - vi.y, v2 = vj.z - vi.z;
@@ -679,7 +690,21 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             w0 += (v1 * p2 - v2 * p1) * wd;
             w1 += (v2 * p0 - v0 * p2) * wd;
             w2 += (v0 * p1 - v1 * p0) * wd;
-        });
+        }
+    };
+    if (ref) {  // the reference's uncapped walk around the final position
+        walk27_batched(
+            d, a.offsets, d.p_off - base, xi,
+            [&](uint32_t j) -> bool {
+                const float4 xj = __ldg(x + j);
+                const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+                const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+                return r2 > 0.f && r2 <= rcut2;
+            },
+            use);
+    } else {  // textbook form over the step's neighbour list
+        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+    }
     const float mr = d.m * d.inv_rho0;
     a.w[i] = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
     TILE_LOOP_END
@@ -703,18 +728,11 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
     const float4 *__restrict__ x = a.x;
     const float4 *__restrict__ w = a.w;
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-    walk27_batched(
-        d, a.offsets, d.p_off - base, xi,
-        [&](uint32_t j) -> bool {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-            return r2 > 0.f && r2 <= rcut2;
-        },
-        [&](uint32_t j) {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+    auto use = [&](uint32_t j) {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+        if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
             const float4 wj = __ldg(w + j);
             const float wl = sqrtf(wj.x * wj.x + wj.y * wj.y + wj.z * wj.z);
@@ -722,7 +740,21 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             n0 += f * p0;
             n1 += f * p1;
             n2 += f * p2;
-        });
+        }
+    };
+    if (ref) {
+        walk27_batched(
+            d, a.offsets, d.p_off - base, xi,
+            [&](uint32_t j) -> bool {
+                const float4 xj = __ldg(x + j);
+                const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+                const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
+                return r2 > 0.f && r2 <= rcut2;
+            },
+            use);
+    } else {
+        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+    }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
     float4 v = vs[i];
@@ -775,22 +807,27 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
     const float rcut2 = d.h2 * 1.0001f;
     const float4 *__restrict__ x = a.x;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    walk27_batched(
-        d, a.offsets, d.p_off - base, xi,
-        [&](uint32_t j) -> bool {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            return p0 * p0 + p1 * p1 + p2 * p2 <= rcut2;
-        },
-        [&](uint32_t j) {
-            const float4 xj = __ldg(x + j);
-            const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-            const float W = wpoly6(sqrtf(p0 * p0 + p1 * p1 + p2 * p2), inv_h, alpha6);
-            const float4 vj = __ldg(vs + j);
-            s0 += (vj.x - vi.x) * W;
-            s1 += (vj.y - vi.y) * W;
-            s2 += (vj.z - vi.z) * W;
-        });
+    auto use = [&](uint32_t j) {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        const float W = wpoly6(sqrtf(p0 * p0 + p1 * p1 + p2 * p2), inv_h, alpha6);
+        const float4 vj = __ldg(vs + j);
+        s0 += (vj.x - vi.x) * W;
+        s1 += (vj.y - vi.y) * W;
+        s2 += (vj.z - vi.z) * W;
+    };
+    if (d.xsph_mode == 1) {  // the reference's uncapped walk
+        walk27_batched(
+            d, a.offsets, d.p_off - base, xi,
+            [&](uint32_t j) -> bool {
+                const float4 xj = __ldg(x + j);
+                const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+                return p0 * p0 + p1 * p1 + p2 * p2 <= rcut2;
+            },
+            use);
+    } else {  // over the step's neighbour list
+        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+    }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
         const float c = d.xsph_c * d.m * d.inv_rho0;

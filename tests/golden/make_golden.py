@@ -83,8 +83,11 @@ def boundary_arrays(sc, mode):
     if mode == "builtin":
         return z4, z4, z3, z3, 0
     if mode == "spheres":
-        inner = np.array([[1.0, 1.0, 1.0, 0.9]], np.float32)
-        outer = np.array([[1.0, 0.2, 1.0, 0.15]], np.float32)
+        # two overlapping spheres that each hold most of the block, so the
+        # projections are moderate (the reference routes outer spheres through
+        # its inner-sphere routine, pbf_response_collision.cu:49)
+        inner = np.array([[0.7, 0.7, 0.5, 0.52]], np.float32)
+        outer = np.array([[0.66, 0.68, 0.48, 0.55]], np.float32)
         return inner, outer, sc.planes[0], sc.planes[1], 1
     raise ValueError(mode)
 
