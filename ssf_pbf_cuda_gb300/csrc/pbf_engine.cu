@@ -8,7 +8,6 @@
 
 namespace pbf103 {
 
-uint32_t blocks_per_sm(uint32_t tile, uint32_t chunk);  // pbf_kernels.cu
 void set_last_error(const char *what, cudaError_t e);
 
 #define CK(call)                                      \
@@ -610,10 +609,14 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     LaunchShape sh;
     sh.tile = tile;
     sh.chunk = chunk_;
-    const uint32_t bps = std::max<uint32_t>(1, blocks_per_sm(tile, chunk_));
-    const uint32_t full = (uint32_t)sms_ * bps;
+    const Occupancy o = occupancy(tile, chunk_);
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
-    sh.grid = std::min(full, nt);
+    auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), nt); };
+    sh.grid = g(o.light);
+    sh.grid_nb = g(o.nb);
+    sh.grid_lambda = g(o.lambda);
+    sh.grid_dp = g(o.dp);
+    sh.grid_list = g(o.list);
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     return sh;
@@ -665,10 +668,7 @@ pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
         k.iters = iters;
         k.xsph = xsph;
         k.vort = vort;
-        k.tile = sh.tile;
-        k.grid = sh.grid;
-        k.scan_grid = sh.scan_grid;
-        k.chunk = sh.chunk;
+        k.shape = sh;
         if (!exec_ || !(k == key_)) {
             if (exec_) {
                 cudaGraphExecDestroy(exec_);

@@ -144,11 +144,10 @@ private:
     struct GraphKey {
         int iters = -1;
         bool xsph = false, vort = false;
-        uint32_t tile = 0, grid = 0, scan_grid = 0, chunk = 0;
+        LaunchShape shape{};
         bool operator==(const GraphKey &o) const
         {
-            return iters == o.iters && xsph == o.xsph && vort == o.vort && tile == o.tile && grid == o.grid &&
-                   scan_grid == o.scan_grid && chunk == o.chunk;
+            return iters == o.iters && xsph == o.xsph && vort == o.vort && shape == o.shape;
         }
     } key_;
     uint32_t last_launches_ = 0;

@@ -84,10 +84,24 @@ struct StepArgs {
 
 struct LaunchShape {
     uint32_t tile;        // particles per tile = threads per block
-    uint32_t grid;        // persistent grid (blocks) for tile kernels
+    uint32_t grid;        // persistent grid (blocks) for the light tile kernels
     uint32_t scan_grid;   // grid for the scan kernels
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
+    // persistent grids of the heavy kernels, each from its own occupancy
+    uint32_t grid_nb, grid_lambda, grid_dp, grid_list;
+    bool operator==(const LaunchShape &o) const
+    {
+        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
+               grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
+               grid_list == o.grid_list;
+    }
 };
+
+// Resident blocks per SM of each kernel class at a tile size / chunk.
+struct Occupancy {
+    uint32_t light, nb, lambda, dp, list;
+};
+Occupancy occupancy(uint32_t tile, uint32_t chunk);
 
 // Called after every kernel launch of a step (per-kernel event timing).
 struct StepHook {

@@ -219,6 +219,59 @@ __device__ __forceinline__ void walk27(const SceneDesc &d, const uint32_t *__res
     }
 }
 
+// walk27 restricted to cells that can hold a particle within h of xp (the
+// binned position): a cell, or a whole row of three, whose nearest point is
+// farther than h holds no accepted candidate, so skipping it leaves the
+// visited sequence of accepted candidates unchanged.  A 1e-3 relative margin
+// covers the rounding of the cell assignment.  With fewer than 4 cells on an
+// axis the reference visits wrapped cells more than once; then the full walk
+// runs.
+template <class F>
+__device__ __forceinline__ void walk27_pruned(const SceneDesc &d, const uint32_t *__restrict__ offsets,
+                                              uint32_t shift, float4 xp, F &&f)
+{
+    if (d.gx < 4 || d.gy < 4 || d.gz < 4) {
+        walk27(d, offsets, shift, xp, f);
+        return;
+    }
+    const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
+    const float lx = xp.x - (float)icx * d.cw, ly = xp.y - (float)icy * d.cw, lz = xp.z - (float)icz * d.cw;
+    const float rx = d.cw - lx, ry = d.cw - ly, rz = d.cw - lz;
+    const float lim = d.h2 * 1.001f;
+    const uint32_t gx = (uint32_t)icx, gy = (uint32_t)icy, gz = (uint32_t)icz;
+    const uint32_t *off = offsets + d.c_off;
+    const uint32_t mx = d.gx - 1u;
+    const uint32_t x0c = (gx - 1u) & mx, x1c = gx & mx, x2c = (gx + 1u) & mx;
+    const bool contiguous = (x2c == x0c + 2u);
+    for (int dz = -1; dz <= 1; ++dz) {
+        const float ez = dz < 0 ? lz : (dz > 0 ? rz : 0.f);
+        for (int dy = -1; dy <= 1; ++dy) {
+            const float ey = dy < 0 ? ly : (dy > 0 ? ry : 0.f);
+            const float eyz2 = ey * ey + ez * ez;
+            if (eyz2 > lim) continue;
+            const bool left = eyz2 + lx * lx <= lim, right = eyz2 + rx * rx <= lim;
+            const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
+                                 ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
+            if (contiguous) {
+                const uint32_t first = left ? x0c : x1c, last = right ? x2c : x1c;
+                const uint32_t st = __ldg(off + row + first) + shift;
+                const uint32_t en = __ldg(off + row + last + 1u) + shift;
+                for (uint32_t q = st; q != en; ++q)
+                    if (!f(q)) return;
+            } else {
+                for (int dx = -1; dx <= 1; ++dx) {
+                    if ((dx < 0 && !left) || (dx > 0 && !right)) continue;
+                    const uint32_t xc = (gx + (uint32_t)dx) & mx;
+                    const uint32_t st = __ldg(off + row + xc) + shift;
+                    const uint32_t en = __ldg(off + row + xc + 1u) + shift;
+                    for (uint32_t q = st; q != en; ++q)
+                        if (!f(q)) return;
+                }
+            }
+        }
+    }
+}
+
 // walk27 with the per-neighbour work taken out of the walk: candidates that
 // pass accept(j) are queued in a small per-thread buffer and handed to use(j)
 // in batches, so the neighbour math is not executed masked for every
@@ -487,7 +540,7 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
     // different candidates, so pair math inside the walk would run masked
     // for almost every candidate)
     uint32_t cnt = 0;
-    walk27(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
+    walk27_pruned(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
         if (dist2_exact(xp, __ldg(xa + q)) < h2) {
             nl[(uint64_t)cnt * stride] = q;
             ++cnt;
@@ -897,20 +950,22 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 }  // namespace
 
 // Resident blocks per SM for the heaviest tile kernels at this block size.
-uint32_t blocks_per_sm(uint32_t tile, uint32_t chunk)
+Occupancy occupancy(uint32_t tile, uint32_t chunk)
 {
-    int a = 0, b = 0, c = 0;
-    if (chunk == 4) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp<4>, (int)tile, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda<4>, (int)tile, 0);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dp<8>, (int)tile, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_lambda<8>, (int)tile, 0);
-    }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_neighbors_lambda, (int)tile, 0);
-    int m = a < b ? a : b;
-    m = m < c ? m : c;
-    return m > 0 ? (uint32_t)m : 1u;
+    auto occ = [tile](const void *fn) -> uint32_t {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, (int)tile, 0);
+        return b > 0 ? (uint32_t)b : 1u;
+    };
+    auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
+    Occupancy o;
+    o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
+                 mn(occ((const void *)k_rank_reorder), occ((const void *)k_finalize)));
+    o.nb = occ((const void *)k_neighbors_lambda);
+    o.dp = chunk == 4 ? occ((const void *)k_dp<4>) : occ((const void *)k_dp<8>);
+    o.lambda = chunk == 4 ? occ((const void *)k_lambda<4>) : occ((const void *)k_lambda<8>);
+    o.list = mn(mn(occ((const void *)k_vort_omega), occ((const void *)k_vort_apply)), occ((const void *)k_xsph));
+    return o;
 }
 
 void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st)
@@ -959,20 +1014,20 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
     PBF_LAUNCHED("k_scatter");
     k_rank_reorder<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_rank_reorder");
-    k_neighbors_lambda<<<g, b, 0, st>>>(a);
+    k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
     PBF_LAUNCHED("k_neighbors_lambda");
     float4 *vfinal = xsph ? a.vt : a.v;
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            if (sh.chunk == 4) k_lambda<4><<<g, b, 0, st>>>(a, cur);
-            else k_lambda<8><<<g, b, 0, st>>>(a, cur);
+            if (sh.chunk == 4) k_lambda<4><<<sh.grid_lambda, b, 0, st>>>(a, cur);
+            else k_lambda<8><<<sh.grid_lambda, b, 0, st>>>(a, cur);
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        if (sh.chunk == 4) k_dp<4><<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
-        else k_dp<8><<<g, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        if (sh.chunk == 4) k_dp<4><<<sh.grid_dp, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        else k_dp<8><<<sh.grid_dp, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;
@@ -983,13 +1038,13 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
         PBF_LAUNCHED("k_finalize");
     }
     if (vort) {
-        k_vort_omega<<<g, b, 0, st>>>(a, vfinal);
+        k_vort_omega<<<sh.grid_list, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega");
-        k_vort_apply<<<g, b, 0, st>>>(a, vfinal);
+        k_vort_apply<<<sh.grid_list, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply");
     }
     if (xsph) {
-        k_xsph<<<g, b, 0, st>>>(a, a.vt, a.v);
+        k_xsph<<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph");
     }
 #undef PBF_LAUNCHED
