@@ -184,6 +184,25 @@ pbf_status pbf_set_graph_mode(pbf_handle *h, int enable);
 pbf_status pbf_get_neighbor_debug(pbf_handle *h, uint32_t *sorted_hash, uint32_t *perm, uint32_t *cell_start,
                                   uint32_t *cell_end, uint32_t *neighbor_list, uint32_t *n_in);
 
+/* ---- neighbour-search sort without allocation ----
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need the sort (code running under CUDA-graph stream
+ * capture, plug-ins whose host owns all device allocations, real-time paths):
+ * cell hash of x (n x 3 floats, device), stable counting sort by cell, and
+ * cell ranges, exactly as pbf_one_step computes them for its predicted
+ * positions.  perm_dev[n] receives sorted -> input index; cell_start_dev /
+ * cell_end_dev [Gx*Gy*Gz] the ranges (0xFFFFFFFF for empty cells).  Needs no
+ * handle and allocates nothing: its scratch is a fixed device array (7.3 MB)
+ * that every GPU loading the library holds until exit.  Larger inputs return
+ * PBF_ERROR_CAPACITY.  The first call on a device looks the array up and
+ * should come before any stream capture; calls that overlap on the GPU share
+ * the array and race, so the caller serialises them. */
+#define PBF_NOALLOC_MAX_PARTICLES 262144u
+#define PBF_NOALLOC_MAX_CELLS 524288u
+pbf_status pbf_cell_sort_noalloc(const float *x_dev, uint32_t n, float cell_width, const uint32_t grid[3],
+                                 uint32_t *perm_dev, uint32_t *cell_start_dev, uint32_t *cell_end_dev,
+                                 void *stream);
+
 /* ---- batched engine: many independent scenes, one launch per kernel per step ---- */
 pbf_status pbf_batch_create(uint32_t max_scenes, uint64_t max_particles, uint64_t max_cells, uint32_t max_pair,
                             int device, pbf_batch **out);

@@ -98,6 +98,7 @@ SIGNATURES = {
     "pbf_last_launches": (c_i32, [c_vp, P(c_u32)]),
     "pbf_profile_step": (c_i32, [c_vp, c_vp, P(c_f), P(c_f), ctypes.c_int, c_vp, P(c_f), c_vp, c_u32, P(c_u32)]),
     "pbf_batch_profile_step": (c_i32, [c_vp, ctypes.c_int, c_vp, P(c_f), c_vp, c_u32, P(c_u32)]),
+    "pbf_cell_sort_noalloc": (c_i32, [c_vp, c_u32, c_f, P(c_u32), c_vp, c_vp, c_vp, c_vp]),
     "pbf_batch_create": (c_i32, [c_u32, c_u64, c_u64, c_u32, ctypes.c_int, P(c_vp)]),
     "pbf_batch_destroy": (c_i32, [c_vp]),
     "pbf_scene_bytes": (c_i32, [P(PbfParams), c_u32, P(c_f), P(c_u64)]),
