@@ -212,6 +212,40 @@ def run_serving(api, args, device: int) -> dict:
     }
 
 
+SORT_KERNELS = ("k_predict_hash", "k_scan_reduce", "k_scan_spine", "k_scan_down", "k_scatter", "k_rank_reorder")
+
+
+def run_ns_microbench(api, device: int, reps: int = 3) -> dict:
+    """Neighbour-search micro-benchmark: 4,194,304 particles over 2^22 cells,
+    (a) uniform and (b) 64 Gaussian blobs; cell hash + stable counting sort +
+    cell ranges (the kernels of the step up to the reorder), timed with CUDA
+    events per kernel.  Algorithmic bytes: 52 + 76 per particle + 20 per cell."""
+    import numpy as np
+
+    from ssf_pbf_cuda_gb300 import scenes
+    out = {}
+    peak, _ = measured_peak_hbm()
+    for kind in ("uniform", "blobs"):
+        x, grid, cw = scenes.config3(kind)
+        p = api.default_params(body_force=[0.0, 0.0, 0.0], grid_size=list(grid), cell_width=cw, smoothing_length=cw)
+        part = api.PbfParticle(p, len(x), (1.0, 1.0, 1.0), device=device)
+        part.set_particles(x, np.zeros_like(x))
+        big = ((-1e30,) * 3, (1e30,) * 3)
+        ms = []
+        for r in range(reps + 1):
+            part.set_particles(x, np.zeros_like(x))
+            prof = api.profile_step(part, None, big, 0)
+            if r:
+                ms.append(sum(t for name, t in prof if name in SORT_KERNELS))
+        t = float(np.median(ms))
+        C = int(np.prod(grid))
+        alg = (52 + 76) * len(x) + 20 * C
+        out[kind] = {"particles": len(x), "cells": C, "ms": t, "particles_per_s": len(x) / (t / 1e3),
+                     "alg_GBps": alg / (t / 1e3) / 1e9, "frac_of_hbm_peak": alg / (t / 1e3) / 1e9 / peak}
+        del part
+    return out
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -476,6 +510,10 @@ def main():
     if rank == 0 and args.serve_seconds > 0:
         serving = run_serving(api, args, local)
 
+    ns_micro = None
+    if rank == 0 and not args.no_plain:
+        ns_micro = run_ns_microbench(api, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v_cpu, sample, cores = cpu_baseline_sample(scs, scene_params, 10.0)
@@ -494,7 +532,7 @@ def main():
                        "step_definition": "device-resident initial state re-loaded, then one full step",
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
-            "serving": serving,
+            "serving": serving, "ns_microbench": ns_micro,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
         }

@@ -1,0 +1,88 @@
+"""Full-size workloads on the GPU, checked against the oracle where it is
+fast (hash + stable counting sort in C) and through size-independent
+properties elsewhere."""
+import numpy as np
+import pytest
+
+from ssf_pbf_cuda_gb300 import api, scenes
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_sort_only(x, grid, cw):
+    """The step's sort of x itself: zero velocity and gravity, no iterations."""
+    p = api.default_params(body_force=[0.0, 0.0, 0.0], grid_size=list(grid), cell_width=cw, smoothing_length=cw)
+    part = api.PbfParticle(p, len(x), (1.0, 1.0, 1.0))
+    part.set_particles(x, np.zeros_like(x))
+    api.one_step(part, None, ((-1e30,) * 3, (1e30,) * 3), 0)
+    return part.neighbor_debug()
+
+
+@pytest.mark.parametrize("kind", ["uniform", "blobs"])
+def test_config3_neighbour_search_bit_exact(oracle, gpu, kind):
+    """4,194,304 particles over 2^22 cells: hashes, stable permutation and
+    cell ranges equal the oracle's stable counting sort."""
+    x, grid, cw = scenes.config3(kind)
+    d = gpu_sort_only(x, grid, cw)
+    keys, perm, off = oracle.hash_sort(x, cw, grid)
+    C = int(np.prod(grid))
+    assert np.array_equal(d["perm"], perm)
+    assert np.array_equal(d["sorted_hash"], keys[perm])
+    ne = off[1:C + 1] > off[:C]
+    assert np.array_equal(d["cell_start"] != 0xFFFFFFFF, ne)
+    assert np.array_equal(d["cell_start"][ne], off[:C][ne]) and np.array_equal(d["cell_end"][ne], off[1:C + 1][ne])
+    # size-independent properties
+    assert np.all(np.diff(d["sorted_hash"].astype(np.int64)) >= 0)
+    assert np.array_equal(np.sort(d["perm"]), np.arange(len(x), dtype=np.uint32))
+
+
+def test_config2_single_large_step_properties(oracle, gpu):
+    """1,048,576 particles, 2^21-cell table: the integer pipeline is bit-exact
+    against the oracle and the permutation is a permutation."""
+    sc = scenes.config2()
+    params = api.config_params()
+    g = H.run_gpu(sc, params, "planes", iters=1)
+    r = H.run_oracle(oracle, sc, params, "planes", iters=1)
+    H.assert_integer_parity(g, r, H.resolved(params, sc))
+    assert np.array_equal(np.sort(g["perm"]), np.arange(sc.n, dtype=np.uint32))
+
+
+def test_long_run_statistics_match_fp64_oracle(oracle, gpu):
+    """A 60-step dam break with stable parameters (64 neighbour slots, s_corr
+    k = 1e-4): mean density error and kinetic energy stay within 1% of the
+    FP64 oracle run in lock step from the same start."""
+    sc = scenes.dam_break(16, 16, 16, (2.0, 1.5, 1.5), scene_id=77)
+    params = api.config_params(scorr_k=1e-4, max_pair_particle_num=64)
+    p = H.resolved(params, sc)
+    part = api.PbfParticle(p, sc.n, sc.domain_end)
+    part.set_particles(sc.x, sc.v)
+    b = H.gpu_boundary(sc, "planes")
+    xo, vo = sc.x, sc.v
+    for _ in range(60):
+        api.one_step(part, b, sc.area, 4)
+        r = H.run_oracle(oracle, sc, params, "planes", 4, f64=True, x=xo, v=vo)
+        xo, vo = r["x"], r["v"]
+    xg, vg = part.get_particles()
+    m = p["particle_mass"]
+
+    def kinetic(v):
+        return 0.5 * m * float((v.astype(np.float64) ** 2).sum())
+
+    def mean_density_error(x):
+        # density from the oracle's neighbour lists of this configuration (one more step, 0 iterations)
+        rr = oracle.step(p, None, (-1e9,) * 3, (1e9,) * 3, 0, x, np.zeros_like(x), f64=True)
+        x0 = np.asarray(x, np.float64)[rr["perm"][:rr["num"]]]
+        h = p["smoothing_length"]
+        rho = np.zeros(len(x0))
+        for k in range(rr["nbr"].shape[1]):
+            sel = rr["nnb"] > k
+            q = rr["nbr"][sel, k]
+            d2 = ((x0[sel] - x0[q]) ** 2).sum(axis=1)
+            rho[sel] += m * 1.56668147065 / h ** 3 * np.clip(1 - d2 / h ** 2, 0, None) ** 3
+        return float(np.abs(rho / p["stable_density"] - 1).mean())
+
+    ke_g, ke_o = kinetic(vg), kinetic(vo)
+    assert abs(ke_g - ke_o) <= 0.01 * ke_o
+    de_g, de_o = mean_density_error(xg), mean_density_error(xo)
+    assert abs(de_g - de_o) <= 0.01 * max(de_o, 1e-6) + 1e-4
