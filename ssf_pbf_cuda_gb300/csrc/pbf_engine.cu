@@ -609,7 +609,8 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     LaunchShape sh;
     sh.tile = tile;
     sh.chunk = chunk_;
-    const Occupancy o = occupancy(tile, chunk_);
+    sh.tpp = tpp_;
+    const Occupancy o = occupancy(tile, chunk_, tpp_);
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
     auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), nt); };
     sh.grid = g(o.light);
@@ -907,6 +908,7 @@ pbf_status Batch::export_x_device(uint32_t id, float *x_dev, cudaStream_t st)
 pbf_status Batch::set_tile(uint32_t tile)
 {
     if (tile != 64 && tile != 128 && tile != 256 && tile != 512) return PBF_ERROR_INVALID_ARGUMENT;
+    if (tile * tpp_ > 1024) return PBF_ERROR_INVALID_ARGUMENT;
     if (tile != tile_) {
         tile_ = tile;
         dirty_tiles_ = true;
@@ -918,6 +920,14 @@ pbf_status Batch::set_chunk(uint32_t chunk)
 {
     if (chunk != 4 && chunk != 8) return PBF_ERROR_INVALID_ARGUMENT;
     chunk_ = chunk;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_tpp(uint32_t tpp)
+{
+    if (tpp != 1 && tpp != 2 && tpp != 4) return PBF_ERROR_INVALID_ARGUMENT;
+    if (tile_ * tpp > 1024) return PBF_ERROR_INVALID_ARGUMENT;
+    tpp_ = tpp;
     return PBF_SUCCESS;
 }
 
@@ -959,6 +969,7 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
     float best_ms = 1e30f;
     for (uint32_t t : cands)
     for (uint32_t ch : chunks) {
+        if (t * tpp_ > 1024) continue;
         set_tile(t);
         chunk_ = ch;
         rc = upload(st);

@@ -84,8 +84,12 @@ public:
     pbf_status profile_step(int iters, cudaStream_t st, float *ms, char *names, uint32_t max, uint32_t *n);
     pbf_status set_tile(uint32_t tile);
     pbf_status set_chunk(uint32_t chunk);
+    // threads per particle in the lambda / delta-p passes; changes the
+    // summation order, so every batch and handle of a process should agree
+    pbf_status set_tpp(uint32_t tpp);
     uint32_t tile() const { return tile_; }
     uint32_t chunk() const { return chunk_; }
+    uint32_t tpp() const { return tpp_; }
     void set_graph_mode(bool on) { graph_mode_ = on; }
     uint32_t last_launches() const { return last_launches_; }
     uint32_t num_scenes() const;
@@ -138,6 +142,7 @@ private:
     // launch configuration and graph cache
     uint32_t tile_ = 256;
     uint32_t chunk_ = 8;
+    uint32_t tpp_ = kDefaultTpp;
     bool graph_mode_ = true;
     cudaStream_t cap_stream_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;

@@ -87,21 +87,22 @@ struct LaunchShape {
     uint32_t grid;        // persistent grid (blocks) for the light tile kernels
     uint32_t scan_grid;   // grid for the scan kernels
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
+    uint32_t tpp;         // threads sharing one particle in the lambda / delta-p passes (1, 2, 4)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_list;
     bool operator==(const LaunchShape &o) const
     {
-        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
+        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk && tpp == o.tpp &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_list == o.grid_list;
     }
 };
 
-// Resident blocks per SM of each kernel class at a tile size / chunk.
+// Resident blocks per SM of each kernel class at a tile size / chunk / tpp.
 struct Occupancy {
     uint32_t light, nb, lambda, dp, list;
 };
-Occupancy occupancy(uint32_t tile, uint32_t chunk);
+Occupancy occupancy(uint32_t tile, uint32_t chunk, uint32_t tpp);
 
 // Called after every kernel launch of a step (per-kernel event timing).
 struct StepHook {
@@ -126,6 +127,10 @@ void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pac
                    const float *src_v, cudaStream_t st);
 void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, float *dst_x, float *dst_v,
                  cudaStream_t st);
+
+// Threads per particle of the lambda / delta-p passes unless a batch sets
+// its own; every handle uses it, so plain and batched steps agree bitwise.
+constexpr uint32_t kDefaultTpp = 2;
 
 constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;

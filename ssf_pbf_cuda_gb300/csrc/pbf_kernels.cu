@@ -307,6 +307,30 @@ __device__ __forceinline__ void prefetch_idx(const uint32_t *__restrict__ nl, ui
     for (int c = 0; c < kChunk; ++c) q[c] = (k0 + c < nn) ? __ldg(nl + (uint64_t)(k0 + c) * stride) : 0u;
 }
 
+// The same for one of TPP threads sharing a particle: thread `sub` takes
+// list slots sub, sub + TPP, sub + 2 TPP, ...; this requests the j0-th to
+// (j0 + kChunk - 1)-th of them.
+template <int kChunk, int TPP>
+__device__ __forceinline__ void prefetch_idx_sub(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t j0,
+                                                 uint32_t sub, uint32_t nn, uint32_t (&q)[kChunk])
+{
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+        const uint32_t k = sub + TPP * (j0 + c);
+        q[c] = (k < nn) ? __ldg(nl + (uint64_t)k * stride) : 0u;
+    }
+}
+
+// Sum v over the TPP threads of a particle group (lanes sub = 0..TPP-1 are
+// consecutive); every lane of the warp must call it.
+template <int TPP>
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = TPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // Visit the listed neighbours of one particle in list order, indices
 // prefetched CH at a time.
 template <int CH, class F>
@@ -569,49 +593,65 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
 // lambda for iterations >= 1 (memorizeKernelCalc + calcScalingFactor,
 // pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
 // per-pair cache: W and grad W are recomputed from positions).
-template <int kChunk>
-__global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__restrict__ xc)
+// TPP threads share one particle (block = tile * TPP threads): thread `sub`
+// sums list slots sub, sub + TPP, ..., and the group adds its partial sums
+// with shuffles, so each particle has TPP independent chains of loads in
+// flight.  No thread leaves the tile loop early: the shuffles need the whole
+// warp.
+template <int kChunk, int TPP>
+__global__ void __launch_bounds__(1024) k_lambda(StepArgs a, const float4 *__restrict__ xc)
 {
-    TILE_LOOP_BEGIN
-    const SceneDesc d = a.scenes[s];
-    const uint32_t base = a.offsets[d.c_off];
-    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
-    if (local >= live) continue;
-    const uint32_t i = d.p_off + local;
-    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-    const float4 xp = xc[i];
-    const uint32_t nn = a.nnb[i];
-    const uint64_t stride = a.nbr_stride;
-    const uint32_t *nl = a.nbr + i;
-    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-    // chunks of kChunk neighbours: the next chunk's indices are requested
-    // before this chunk's positions, so index and position latencies overlap
-    uint32_t qn[kChunk];
-    prefetch_idx(nl, stride, 0, nn, qn);
-    for (uint32_t k0 = 0; k0 < nn; k0 += kChunk) {
-        uint32_t q[kChunk];
+    const uint32_t n_tiles = a.ctrl->n_tiles;
+    const uint32_t sub = threadIdx.x % TPP;
+    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const uint32_t s = __ldg(a.tile_scene + t);
+        const uint32_t local = __ldg(a.tile_start + t) + threadIdx.x / TPP;
+        const SceneDesc d = a.scenes[s];
+        const uint32_t base = a.offsets[d.c_off];
+        const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+        const bool active = local < live;
+        const uint32_t i = d.p_off + (active ? local : 0u);
+        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+        const float4 xp = active ? xc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t nn = active ? a.nnb[i] : 0u;
+        const uint64_t stride = a.nbr_stride;
+        const uint32_t *nl = a.nbr + i;
+        float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+        // chunks of kChunk of this thread's slots: the next chunk's indices
+        // are requested before this chunk's positions
+        uint32_t qn[kChunk];
+        prefetch_idx_sub<kChunk, TPP>(nl, stride, 0, sub, nn, qn);
+        for (uint32_t j0 = 0; sub + TPP * j0 < nn; j0 += kChunk) {
+            uint32_t q[kChunk];
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
-        prefetch_idx(nl, stride, k0 + kChunk, nn, qn);
-        float4 xq[kChunk];
+            for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
+            prefetch_idx_sub<kChunk, TPP>(nl, stride, j0 + kChunk, sub, nn, qn);
+            float4 xq[kChunk];
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) xq[c] = (k0 + c < nn) ? __ldg(xc + q[c]) : xp;
+            for (int c = 0; c < kChunk; ++c) xq[c] = (sub + TPP * (j0 + c) < nn) ? __ldg(xc + q[c]) : xp;
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) {
-            if (k0 + c < nn) {
-                const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
-                ks += pk.W;
-                g0 += pk.gx;
-                g1 += pk.gy;
-                g2 += pk.gz;
-                kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+            for (int c = 0; c < kChunk; ++c) {
+                if (sub + TPP * (j0 + c) < nn) {
+                    const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
+                    ks += pk.W;
+                    g0 += pk.gx;
+                    g1 += pk.gy;
+                    g2 += pk.gz;
+                    kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+                }
             }
         }
+        ks = group_sum<TPP>(ks);
+        g0 = group_sum<TPP>(g0);
+        g1 = group_sum<TPP>(g1);
+        g2 = group_sum<TPP>(g2);
+        kg2 = group_sum<TPP>(kg2);
+        if (active && sub == 0) {
+            const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
+            const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+            a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+        }
     }
-    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
-    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
-    TILE_LOOP_END
 }
 
 // delta-p with s_corr (calcPositionUpdateCUDA cached, pbf_position_update.cu:131-188),
@@ -620,77 +660,87 @@ __global__ void __launch_bounds__(512) k_lambda(StepArgs a, const float4 *__rest
 // buffer so neighbours still read the old positions.  On the last iteration
 // the velocity update (updateVelocityCUDA, pbf_update.cu:25-39) is fused in:
 // v = (x_new - x_old) / dt, written with x_new to the particle phase.
-template <int kChunk>
-__global__ void __launch_bounds__(512) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
-                                          float4 *__restrict__ vo, int last)
+template <int kChunk, int TPP>
+__global__ void __launch_bounds__(1024) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
+                                           float4 *__restrict__ vo, int last)
 {
-    TILE_LOOP_BEGIN
-    const SceneDesc d = a.scenes[s];
-    const uint32_t base = a.offsets[d.c_off];
-    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
-    if (last && local == 0) a.scene_num[s] = live;
-    if (local >= live) continue;
-    const uint32_t i = d.p_off + local;
-    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-    const float4 xp = xc[i];
-    const float li = a.lam[i];
-    const float sci = (li < 0.f) ? -li : 0.f;
-    const int mode = d.tensile_mode;
-    const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
-    const int sn = d.scorr_n;
-    const uint32_t nn = a.nnb[i];
-    const uint64_t stride = a.nbr_stride;
-    const uint32_t *nl = a.nbr + i;
-    const float *__restrict__ lam = a.lam;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    uint32_t qn[kChunk];
-    prefetch_idx(nl, stride, 0, nn, qn);
-    for (uint32_t k0 = 0; k0 < nn; k0 += kChunk) {
-        uint32_t q[kChunk];
+    const uint32_t n_tiles = a.ctrl->n_tiles;
+    const uint32_t sub = threadIdx.x % TPP;
+    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const uint32_t s = __ldg(a.tile_scene + t);
+        const uint32_t local = __ldg(a.tile_start + t) + threadIdx.x / TPP;
+        const SceneDesc d = a.scenes[s];
+        const uint32_t base = a.offsets[d.c_off];
+        const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+        if (last && local == 0 && sub == 0) a.scene_num[s] = live;
+        const bool active = local < live;
+        const uint32_t i = d.p_off + (active ? local : 0u);
+        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+        const float4 xp = active ? xc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float li = active ? a.lam[i] : 0.f;
+        const float sci = (li < 0.f) ? -li : 0.f;
+        const int mode = d.tensile_mode;
+        const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
+        const int sn = d.scorr_n;
+        const uint32_t nn = active ? a.nnb[i] : 0u;
+        const uint64_t stride = a.nbr_stride;
+        const uint32_t *nl = a.nbr + i;
+        const float *__restrict__ lam = a.lam;
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        uint32_t qn[kChunk];
+        prefetch_idx_sub<kChunk, TPP>(nl, stride, 0, sub, nn, qn);
+        for (uint32_t j0 = 0; sub + TPP * j0 < nn; j0 += kChunk) {
+            uint32_t q[kChunk];
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
-        prefetch_idx(nl, stride, k0 + kChunk, nn, qn);
-        float4 xq[kChunk];
-        float lq[kChunk];
+            for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
+            prefetch_idx_sub<kChunk, TPP>(nl, stride, j0 + kChunk, sub, nn, qn);
+            float4 xq[kChunk];
+            float lq[kChunk];
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) {
-            const bool ok = k0 + c < nn;
-            xq[c] = ok ? __ldg(xc + q[c]) : xp;
-            lq[c] = ok ? __ldg(lam + q[c]) : 0.f;
-        }
+            for (int c = 0; c < kChunk; ++c) {
+                const bool ok = sub + TPP * (j0 + c) < nn;
+                xq[c] = ok ? __ldg(xc + q[c]) : xp;
+                lq[c] = ok ? __ldg(lam + q[c]) : 0.f;
+            }
 #pragma unroll
-        for (int c = 0; c < kChunk; ++c) {
-            if (k0 + c < nn) {
-                const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
-                const float lj = lq[c];
-                float corr = 0.f;
-                if (mode == PBF_TENSILE_REFERENCE) {
-                    const float kr2 = pk.W * pk.W;
-                    const float tc = 10.f * (kr2 * kr2) * inv_k;
-                    corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
-                } else if (mode == PBF_TENSILE_TEXTBOOK) {
-                    const float ratio = pk.W * inv_wdq;
-                    float pw = 1.f;
-                    for (int e = 0; e < sn; ++e) pw *= ratio;
-                    corr = sk * pw;
+            for (int c = 0; c < kChunk; ++c) {
+                if (sub + TPP * (j0 + c) < nn) {
+                    const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
+                    const float lj = lq[c];
+                    float corr = 0.f;
+                    if (mode == PBF_TENSILE_REFERENCE) {
+                        const float kr2 = pk.W * pk.W;
+                        const float tc = 10.f * (kr2 * kr2) * inv_k;
+                        corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
+                    } else if (mode == PBF_TENSILE_TEXTBOOK) {
+                        const float ratio = pk.W * inv_wdq;
+                        float pw = 1.f;
+                        for (int e = 0; e < sn; ++e) pw *= ratio;
+                        corr = sk * pw;
+                    }
+                    const float cc = -(li + lj + corr);
+                    s0 += cc * pk.gx;
+                    s1 += cc * pk.gy;
+                    s2 += cc * pk.gz;
                 }
-                const float cc = -(li + lj + corr);
-                s0 += cc * pk.gx;
-                s1 += cc * pk.gy;
-                s2 += cc * pk.gz;
+            }
+        }
+        s0 = group_sum<TPP>(s0);
+        s1 = group_sum<TPP>(s1);
+        s2 = group_sum<TPP>(s2);
+        if (active && sub == 0) {
+            float3 dp = make_float3(s0 * d.m * d.inv_rho0, s1 * d.m * d.inv_rho0, s2 * d.m * d.inv_rho0);
+            const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
+            if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
+            const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
+            xo[i] = xn;
+            if (last) {
+                const float4 xo_ = a.xold[i];
+                vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z),
+                                    0.f);
             }
         }
     }
-    float3 dp = make_float3(s0 * d.m * d.inv_rho0, s1 * d.m * d.inv_rho0, s2 * d.m * d.inv_rho0);
-    const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
-    if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
-    const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
-    xo[i] = xn;
-    if (last) {
-        const float4 xo_ = a.xold[i];
-        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
-    }
-    TILE_LOOP_END
 }
 
 // iters == 0: positions stay at the prediction; v from the velocity update.
@@ -949,21 +999,58 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 
 }  // namespace
 
+// The lambda / delta-p variants: neighbour chunk kChunk x threads per
+// particle TPP, selected at run time by (chunk, tpp).
+template <int CH, int TPP>
+struct PassFns {
+    static const void *lambda() { return (const void *)k_lambda<CH, TPP>; }
+    static const void *dp() { return (const void *)k_dp<CH, TPP>; }
+    static void launch_lambda(const StepArgs &a, const LaunchShape &sh, const float4 *cur, cudaStream_t st)
+    {
+        k_lambda<CH, TPP><<<sh.grid_lambda, sh.tile * TPP, 0, st>>>(a, cur);
+    }
+    static void launch_dp(const StepArgs &a, const LaunchShape &sh, const float4 *cur, float4 *out, float4 *vo,
+                          int last, cudaStream_t st)
+    {
+        k_dp<CH, TPP><<<sh.grid_dp, sh.tile * TPP, 0, st>>>(a, cur, out, vo, last);
+    }
+};
+
+#define PBF_PASS_DISPATCH(chunk, tpp, CALL)       \
+    switch ((chunk) * 10 + (tpp)) {               \
+    case 41: PassFns<4, 1>::CALL; break;          \
+    case 42: PassFns<4, 2>::CALL; break;          \
+    case 44: PassFns<4, 4>::CALL; break;          \
+    case 81: PassFns<8, 1>::CALL; break;          \
+    case 82: PassFns<8, 2>::CALL; break;          \
+    default: PassFns<8, 4>::CALL; break;          \
+    }
+
 // Resident blocks per SM for the heaviest tile kernels at this block size.
-Occupancy occupancy(uint32_t tile, uint32_t chunk)
+Occupancy occupancy(uint32_t tile, uint32_t chunk, uint32_t tpp)
 {
-    auto occ = [tile](const void *fn) -> uint32_t {
+    auto occ_b = [](const void *fn, uint32_t block) -> uint32_t {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, (int)tile, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, (int)block, 0);
         return b > 0 ? (uint32_t)b : 1u;
     };
+    auto occ = [&](const void *fn) { return occ_b(fn, tile); };
     auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
     Occupancy o;
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
                  mn(occ((const void *)k_rank_reorder), occ((const void *)k_finalize)));
     o.nb = occ((const void *)k_neighbors_lambda);
-    o.dp = chunk == 4 ? occ((const void *)k_dp<4>) : occ((const void *)k_dp<8>);
-    o.lambda = chunk == 4 ? occ((const void *)k_lambda<4>) : occ((const void *)k_lambda<8>);
+    const void *fl = nullptr, *fd = nullptr;
+    switch (chunk * 10 + tpp) {
+    case 41: fl = PassFns<4, 1>::lambda(); fd = PassFns<4, 1>::dp(); break;
+    case 42: fl = PassFns<4, 2>::lambda(); fd = PassFns<4, 2>::dp(); break;
+    case 44: fl = PassFns<4, 4>::lambda(); fd = PassFns<4, 4>::dp(); break;
+    case 81: fl = PassFns<8, 1>::lambda(); fd = PassFns<8, 1>::dp(); break;
+    case 82: fl = PassFns<8, 2>::lambda(); fd = PassFns<8, 2>::dp(); break;
+    default: fl = PassFns<8, 4>::lambda(); fd = PassFns<8, 4>::dp(); break;
+    }
+    o.lambda = occ_b(fl, tile * tpp);
+    o.dp = occ_b(fd, tile * tpp);
     o.list = mn(mn(occ((const void *)k_vort_omega), occ((const void *)k_vort_apply)), occ((const void *)k_xsph));
     return o;
 }
@@ -1020,14 +1107,12 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            if (sh.chunk == 4) k_lambda<4><<<sh.grid_lambda, b, 0, st>>>(a, cur);
-            else k_lambda<8><<<sh.grid_lambda, b, 0, st>>>(a, cur);
+            PBF_PASS_DISPATCH(sh.chunk, sh.tpp, launch_lambda(a, sh, cur, st));
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        if (sh.chunk == 4) k_dp<4><<<sh.grid_dp, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
-        else k_dp<8><<<sh.grid_dp, b, 0, st>>>(a, cur, out, last ? vfinal : nullptr, last ? 1 : 0);
+        PBF_PASS_DISPATCH(sh.chunk, sh.tpp, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;
