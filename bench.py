@@ -76,7 +76,10 @@ def committed_traffic(kernel: str, workload: str):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms from
+    before the warm-up on; summary() keeps the samples taken between
+    mark_start() and mark_end() (the timed region), or the nearest one when
+    the region is shorter than the sampling interval."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -85,11 +88,12 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.t_start = self.t_end = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -99,7 +103,13 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark_start(self):
+        self.t_start = time.monotonic()
+
+    def mark_end(self):
+        self.t_end = time.monotonic()
 
     def __exit__(self, *a):
         if self.proc:
@@ -109,10 +119,19 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def _window(self):
+        if self.t_start is None or self.t_end is None:
+            return [ln for _, ln in self.lines]
+        inside = [ln for t, ln in self.lines if self.t_start <= t <= self.t_end]
+        if inside or not self.lines:
+            return inside
+        mid = 0.5 * (self.t_start + self.t_end)
+        return [min(self.lines, key=lambda tl: abs(tl[0] - mid))[1]]
+
     def summary(self):
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self._window():
             f = [t.strip() for t in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -127,7 +146,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": 20}
 
 
 def shard_scenes(n_scenes: int, rank: int, world: int):
@@ -138,21 +157,21 @@ def shard_scenes(n_scenes: int, rank: int, world: int):
 
 
 def cpu_baseline_sample(scs, params_fn, seconds: float = 10.0):
-    """The CPU oracle (OpenMP, all host threads) on the first scenes of the
-    workload until about `seconds` of work; returns (particle-steps/s, sample)."""
+    """The CPU oracle (OpenMP, all host threads) stepping the workload's
+    scenes in order, cycling through them again, until about `seconds` of
+    work; returns (particle-steps/s, sample description, threads)."""
     from oracle import oracle as O
     O.build()
+    prepared = [(sc, params_fn(sc), O.Boundary(plane_pts=sc.planes[0], plane_nrm=sc.planes[1])) for sc in scs]
     done, n_sc, t0 = 0, 0, time.perf_counter()
-    for sc in scs:
-        p = params_fn(sc)
-        b = O.Boundary(plane_pts=sc.planes[0], plane_nrm=sc.planes[1])
+    while time.perf_counter() - t0 < seconds:
+        sc, p, b = prepared[n_sc % len(prepared)]
         O.step(p, b, sc.area[0], sc.area[1], ITERS, sc.x, sc.v)
         done += sc.n
         n_sc += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
     dt = time.perf_counter() - t0
-    return done / dt, f"{n_sc} scenes ({done} particles), one step each, {dt:.1f} s", O.num_threads()
+    return done / dt, (f"{n_sc} scene-steps over the first {min(n_sc, len(prepared))} of {len(prepared)} scenes "
+                       f"({done} particle-steps, each from the scene's initial state), {dt:.1f} s"), O.num_threads()
 
 
 def scene_params(sc):
@@ -302,6 +321,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle in the lambda/dp passes (0 = library default)")
+    ap.add_argument("--chunk", type=int, default=0, help="neighbour chunk of the lambda/dp passes (0 = autotune)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="arrival window of the serving run (0 = off)")
     ap.add_argument("--serve-rate", type=float, default=12.0, help="request arrivals per second")
     ap.add_argument("--serve-tile", type=int, default=256)
@@ -347,8 +367,8 @@ def main():
     x0d = torch.from_numpy(x0h).to(dev)
     v0d = torch.from_numpy(v0h).to(dev)
     torch.cuda.synchronize()
-    if args.tpp:
-        batch.set_pass_shape(8, args.tpp)
+    if args.tpp or args.chunk:
+        batch.set_pass_shape(args.chunk or 8, args.tpp or batch.launch_shape()["tpp"])
     tile = args.tile or batch.autotune(ITERS, stream)
     batch.set_tile(tile)
     shape = batch.launch_shape()
@@ -357,19 +377,21 @@ def main():
         batch.set_all(x0d, v0d, counts, stream)
         batch.step(ITERS, stream)
 
-    for _ in range(args.warmup):
-        batched_step()
-    launches_per_step = batch.launches + 1  # + the unpack kernel of set_all
-    torch.cuda.synchronize()
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            batched_step()
+        launches_per_step = batch.launches + 1  # + the unpack kernel of set_all
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clk.mark_start()
         e0.record(stream)
         for _ in range(args.steps):
             batched_step()
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark_end()
     barrier()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)

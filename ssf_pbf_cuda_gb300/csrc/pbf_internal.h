@@ -130,7 +130,7 @@ void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_
 
 // Threads per particle of the lambda / delta-p passes unless a batch sets
 // its own; every handle uses it, so plain and batched steps agree bitwise.
-constexpr uint32_t kDefaultTpp = 2;
+constexpr uint32_t kDefaultTpp = 1;
 
 constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;
