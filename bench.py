@@ -320,7 +320,6 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
-    ap.add_argument("--tpp", type=int, default=0, help="threads per particle in the lambda/dp passes (0 = library default)")
     ap.add_argument("--chunk", type=int, default=0, help="neighbour chunk of the lambda/dp passes (0 = autotune)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="arrival window of the serving run (0 = off)")
     ap.add_argument("--serve-rate", type=float, default=12.0, help="request arrivals per second")
@@ -367,8 +366,8 @@ def main():
     x0d = torch.from_numpy(x0h).to(dev)
     v0d = torch.from_numpy(v0h).to(dev)
     torch.cuda.synchronize()
-    if args.tpp or args.chunk:
-        batch.set_pass_shape(args.chunk or 8, args.tpp or batch.launch_shape()["tpp"])
+    if args.chunk:
+        batch.set_chunk(args.chunk)
     tile = args.tile or batch.autotune(ITERS, stream)
     batch.set_tile(tile)
     shape = batch.launch_shape()
@@ -553,7 +552,7 @@ def main():
             "config": {"workload": f"batched: {len(scs)} dam-break scenes per GPU, 4k-64k particles "
                                    f"(log-uniform, seeded), {ITERS} iterations, s_corr k=0.1 n=4 dq=0.2h, "
                                    "XSPH 0.01, vorticity 0.0005, eps 600, dt 1/120",
-                       "particles_per_gpu": n_total, "cells_per_gpu": cells, "tile": tile, "chunk": shape["chunk"], "tpp": shape["tpp"],
+                       "particles_per_gpu": n_total, "cells_per_gpu": cells, "tile": tile, "chunk": shape["chunk"],
                        "l2": "inputs larger than L2 (per-step working set >> 129 MB)",
                        "step_definition": "device-resident initial state re-loaded, then one full step",
                        "parallelism": f"replicas x{world}"},

@@ -237,14 +237,12 @@ pbf_status pbf_batch_get_all(pbf_batch *b, uint32_t *counts, float *x, float *v,
  * Leaves particle state unchanged. */
 pbf_status pbf_batch_autotune(pbf_batch *b, int iters, void *stream, uint32_t *chosen_tile);
 pbf_status pbf_batch_set_tile(pbf_batch *b, uint32_t tile);
-/* Shape of the lambda / delta-p passes: chunk = neighbour indices fetched
- * ahead per thread (4 or 8); tpp = threads sharing one particle's neighbour
- * list (1, 2 or 4; tile * tpp <= 1024).  tpp changes the floating-point
- * summation order, so batches and handles compared bitwise must share it.
- * No reference counterpart (the reference runs one thread per particle). */
-pbf_status pbf_batch_set_pass_shape(pbf_batch *b, uint32_t chunk, uint32_t tpp);
-/* Current tile (particles per block), chunk and tpp. */
-pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *chunk, uint32_t *tpp);
+/* Neighbour indices requested ahead per thread in the lambda / delta-p
+ * passes (4 or 8; the autotuner also picks it).  Results do not depend on it.
+ * No reference counterpart. */
+pbf_status pbf_batch_set_chunk(pbf_batch *b, uint32_t chunk);
+/* Current tile (particles per block) and chunk. */
+pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *chunk);
 pbf_status pbf_batch_set_graph_mode(pbf_batch *b, int enable);
 /* Kernels launched by the last pbf_batch_step / pbf_one_step call. */
 pbf_status pbf_batch_last_launches(pbf_batch *b, uint32_t *launches);

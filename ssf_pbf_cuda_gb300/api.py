@@ -421,16 +421,15 @@ class Batch:
     def set_tile(self, tile: int):
         check(load().pbf_batch_set_tile(self.handle, int(tile)), "pbf_batch_set_tile")
 
-    def set_pass_shape(self, chunk: int, tpp: int):
-        """Neighbour chunk (4, 8) and threads per particle (1, 2, 4) of the
-        lambda / delta-p passes."""
-        check(load().pbf_batch_set_pass_shape(self.handle, int(chunk), int(tpp)), "pbf_batch_set_pass_shape")
+    def set_chunk(self, chunk: int):
+        """Neighbour indices requested ahead per thread in the lambda / delta-p passes (4 or 8)."""
+        check(load().pbf_batch_set_chunk(self.handle, int(chunk)), "pbf_batch_set_chunk")
 
     def launch_shape(self) -> dict:
-        t, c, p = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
-        check(load().pbf_batch_get_launch_shape(self.handle, ctypes.byref(t), ctypes.byref(c), ctypes.byref(p)),
+        t, c = ctypes.c_uint32(), ctypes.c_uint32()
+        check(load().pbf_batch_get_launch_shape(self.handle, ctypes.byref(t), ctypes.byref(c)),
               "pbf_batch_get_launch_shape")
-        return {"tile": t.value, "chunk": c.value, "tpp": p.value}
+        return {"tile": t.value, "chunk": c.value}
 
     def set_graph_mode(self, on: bool):
         check(load().pbf_batch_set_graph_mode(self.handle, 1 if on else 0), "pbf_batch_set_graph_mode")

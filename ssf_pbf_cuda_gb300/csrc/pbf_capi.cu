@@ -477,22 +477,19 @@ pbf_status pbf_batch_set_tile(pbf_batch *b, uint32_t tile)
     return b->b.set_tile(tile);
 }
 
-pbf_status pbf_batch_set_pass_shape(pbf_batch *b, uint32_t chunk, uint32_t tpp)
+pbf_status pbf_batch_set_chunk(pbf_batch *b, uint32_t chunk)
 {
     if (!b) return PBF_ERROR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(b->mu);
-    pbf_status rc = b->b.set_chunk(chunk);
-    if (rc != PBF_SUCCESS) return rc;
-    return b->b.set_tpp(tpp);
+    return b->b.set_chunk(chunk);
 }
 
-pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *chunk, uint32_t *tpp)
+pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *chunk)
 {
     if (!b) return PBF_ERROR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(b->mu);
     if (tile) *tile = b->b.tile();
     if (chunk) *chunk = b->b.chunk();
-    if (tpp) *tpp = b->b.tpp();
     return PBF_SUCCESS;
 }
 

@@ -609,8 +609,7 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     LaunchShape sh;
     sh.tile = tile;
     sh.chunk = chunk_;
-    sh.tpp = tpp_;
-    const Occupancy o = occupancy(tile, chunk_, tpp_);
+    const Occupancy o = occupancy(tile, chunk_);
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
     auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), nt); };
     sh.grid = g(o.light);
@@ -655,20 +654,35 @@ StepArgs Batch::args() const
     return a;
 }
 
+uint32_t Batch::post_modes() const
+{
+    bool x_off = false, x_walk = false, x_list = false, v_ref = false, v_text = false;
+    for (auto &s : scenes_)
+        if (s.active) {
+            x_off |= s.desc.xsph_mode == PBF_XSPH_OFF;
+            x_walk |= s.desc.xsph_mode == PBF_XSPH_WALK;
+            x_list |= s.desc.xsph_mode == PBF_XSPH_LIST;
+            v_ref |= s.desc.vort_mode == PBF_VORTICITY_REFERENCE;
+            v_text |= s.desc.vort_mode == PBF_VORTICITY_TEXTBOOK;
+        }
+    uint32_t m = 0;
+    if (x_walk) m |= kPostXsphWalk;
+    // the list-form XSPH kernel also copies the velocities of scenes without
+    // XSPH when some scene of the batch has it
+    if (x_list || (x_off && x_walk)) m |= kPostXsphList;
+    if (v_ref) m |= kPostVortReference;
+    if (v_text) m |= kPostVortTextbook;
+    return m;
+}
+
 pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
 {
     const LaunchShape sh = shape_for(tile_);
-    bool xsph = false, vort = false;
-    for (auto &s : scenes_)
-        if (s.active) {
-            xsph |= s.desc.xsph_mode != 0;
-            vort |= s.desc.vort_mode != 0;
-        }
+    const uint32_t modes = post_modes();
     if (allow_graph && graph_mode_) {
         GraphKey k;
         k.iters = iters;
-        k.xsph = xsph;
-        k.vort = vort;
+        k.modes = modes;
         k.shape = sh;
         if (!exec_ || !(k == key_)) {
             if (exec_) {
@@ -676,7 +690,7 @@ pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
                 exec_ = nullptr;
             }
             CK(cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeThreadLocal));
-            graph_launches_ = enqueue_step(args(), sh, iters, xsph, vort, cap_stream_);
+            graph_launches_ = enqueue_step(args(), sh, iters, modes, cap_stream_);
             cudaGraph_t g = nullptr;
             CK(cudaStreamEndCapture(cap_stream_, &g));
             cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
@@ -691,7 +705,7 @@ pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
         CK(cudaGraphLaunch(exec_, st));
         last_launches_ = graph_launches_;
     } else {
-        last_launches_ = enqueue_step(args(), sh, iters, xsph, vort, st);
+        last_launches_ = enqueue_step(args(), sh, iters, modes, st);
     }
     CK(cudaGetLastError());
     return PBF_SUCCESS;
@@ -721,18 +735,12 @@ pbf_status Batch::profile_step(int iters, cudaStream_t st, float *ms, char *name
     if (rc != PBF_SUCCESS) return rc;
     *n = 0;
     if (ctrl_.n_tiles == 0) return PBF_SUCCESS;
-    bool xsph = false, vort = false;
-    for (auto &s : scenes_)
-        if (s.active) {
-            xsph |= s.desc.xsph_mode != 0;
-            vort |= s.desc.vort_mode != 0;
-        }
     EventHook hook;
     hook.st = st;
     cudaEvent_t e0;
     CK(cudaEventCreate(&e0));
     CK(cudaEventRecord(e0, st));
-    last_launches_ = enqueue_step(args(), shape_for(tile_), iters, xsph, vort, st, &hook);
+    last_launches_ = enqueue_step(args(), shape_for(tile_), iters, post_modes(), st, &hook);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     cudaEvent_t prev = e0;
@@ -908,7 +916,6 @@ pbf_status Batch::export_x_device(uint32_t id, float *x_dev, cudaStream_t st)
 pbf_status Batch::set_tile(uint32_t tile)
 {
     if (tile != 64 && tile != 128 && tile != 256 && tile != 512) return PBF_ERROR_INVALID_ARGUMENT;
-    if (tile * tpp_ > 1024) return PBF_ERROR_INVALID_ARGUMENT;
     if (tile != tile_) {
         tile_ = tile;
         dirty_tiles_ = true;
@@ -920,14 +927,6 @@ pbf_status Batch::set_chunk(uint32_t chunk)
 {
     if (chunk != 4 && chunk != 8) return PBF_ERROR_INVALID_ARGUMENT;
     chunk_ = chunk;
-    return PBF_SUCCESS;
-}
-
-pbf_status Batch::set_tpp(uint32_t tpp)
-{
-    if (tpp != 1 && tpp != 2 && tpp != 4) return PBF_ERROR_INVALID_ARGUMENT;
-    if (tile_ * tpp > 1024) return PBF_ERROR_INVALID_ARGUMENT;
-    tpp_ = tpp;
     return PBF_SUCCESS;
 }
 
@@ -969,7 +968,6 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
     float best_ms = 1e30f;
     for (uint32_t t : cands)
     for (uint32_t ch : chunks) {
-        if (t * tpp_ > 1024) continue;
         set_tile(t);
         chunk_ = ch;
         rc = upload(st);

@@ -84,12 +84,8 @@ public:
     pbf_status profile_step(int iters, cudaStream_t st, float *ms, char *names, uint32_t max, uint32_t *n);
     pbf_status set_tile(uint32_t tile);
     pbf_status set_chunk(uint32_t chunk);
-    // threads per particle in the lambda / delta-p passes; changes the
-    // summation order, so every batch and handle of a process should agree
-    pbf_status set_tpp(uint32_t tpp);
     uint32_t tile() const { return tile_; }
     uint32_t chunk() const { return chunk_; }
-    uint32_t tpp() const { return tpp_; }
     void set_graph_mode(bool on) { graph_mode_ = on; }
     uint32_t last_launches() const { return last_launches_; }
     uint32_t num_scenes() const;
@@ -102,6 +98,7 @@ private:
     pbf_status upload(cudaStream_t st);
     pbf_status run(int iters, cudaStream_t st, bool allow_graph);
     LaunchShape shape_for(uint32_t tile) const;
+    uint32_t post_modes() const;  // kPost* bits of the active scenes
     void rebuild_tiles();
     StepArgs args() const;
 
@@ -142,17 +139,16 @@ private:
     // launch configuration and graph cache
     uint32_t tile_ = 256;
     uint32_t chunk_ = 8;
-    uint32_t tpp_ = kDefaultTpp;
     bool graph_mode_ = true;
     cudaStream_t cap_stream_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     struct GraphKey {
         int iters = -1;
-        bool xsph = false, vort = false;
+        uint32_t modes = 0;
         LaunchShape shape{};
         bool operator==(const GraphKey &o) const
         {
-            return iters == o.iters && xsph == o.xsph && vort == o.vort && shape == o.shape;
+            return iters == o.iters && modes == o.modes && shape == o.shape;
         }
     } key_;
     uint32_t last_launches_ = 0;

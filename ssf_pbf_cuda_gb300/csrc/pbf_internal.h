@@ -87,22 +87,21 @@ struct LaunchShape {
     uint32_t grid;        // persistent grid (blocks) for the light tile kernels
     uint32_t scan_grid;   // grid for the scan kernels
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
-    uint32_t tpp;         // threads sharing one particle in the lambda / delta-p passes (1, 2, 4)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_list;
     bool operator==(const LaunchShape &o) const
     {
-        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk && tpp == o.tpp &&
+        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_list == o.grid_list;
     }
 };
 
-// Resident blocks per SM of each kernel class at a tile size / chunk / tpp.
+// Resident blocks per SM of each kernel class at a tile size / chunk.
 struct Occupancy {
     uint32_t light, nb, lambda, dp, list;
 };
-Occupancy occupancy(uint32_t tile, uint32_t chunk, uint32_t tpp);
+Occupancy occupancy(uint32_t tile, uint32_t chunk);
 
 // Called after every kernel launch of a step (per-kernel event timing).
 struct StepHook {
@@ -110,9 +109,17 @@ struct StepHook {
     virtual ~StepHook() = default;
 };
 
+// Post-solve passes a step runs (bit set: some active scene needs that form).
+enum : uint32_t {
+    kPostXsphWalk = 1,       // XSPH, the reference's uncapped 27-cell walk
+    kPostXsphList = 2,       // XSPH over the step's neighbour list (+ copy for scenes without XSPH)
+    kPostVortReference = 4,  // vorticity, the reference's walk and kernel scaling
+    kPostVortTextbook = 8,   // vorticity, textbook form over the neighbour list
+};
+
 // Enqueue one full solver step for every scene in the tile list.
 // Returns the number of kernels launched.
-uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, bool xsph, bool vort,
+uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, uint32_t post_modes,
                       cudaStream_t stream, StepHook *hook = nullptr);
 
 // Edge conversions between the ABI's AoS float3 and the internal float4.
@@ -127,10 +134,6 @@ void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pac
                    const float *src_v, cudaStream_t st);
 void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, float *dst_x, float *dst_v,
                  cudaStream_t st);
-
-// Threads per particle of the lambda / delta-p passes unless a batch sets
-// its own; every handle uses it, so plain and batched steps agree bitwise.
-constexpr uint32_t kDefaultTpp = 1;
 
 constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;

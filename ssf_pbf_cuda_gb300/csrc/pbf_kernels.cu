@@ -296,57 +296,33 @@ __device__ __forceinline__ void walk27_batched(const SceneDesc &d, const uint32_
     for (int k = 0; k < nb; ++k) use(buf[k]);
 }
 
-// Request list slots [k0, k0 + kChunk) of one particle (slot-major layout);
-// slots past nn read nothing.  kChunk (neighbours per chunk in the lambda /
-// delta-p passes) trades registers for loads in flight; the autotuner picks it.
-template <int kChunk>
-__device__ __forceinline__ void prefetch_idx(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t k0,
-                                             uint32_t nn, uint32_t (&q)[kChunk])
-{
-#pragma unroll
-    for (int c = 0; c < kChunk; ++c) q[c] = (k0 + c < nn) ? __ldg(nl + (uint64_t)(k0 + c) * stride) : 0u;
-}
-
-// The same for one of TPP threads sharing a particle: thread `sub` takes
-// list slots sub, sub + TPP, sub + 2 TPP, ...; this requests the j0-th to
-// (j0 + kChunk - 1)-th of them.
-template <int kChunk, int TPP>
-__device__ __forceinline__ void prefetch_idx_sub(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t j0,
-                                                 uint32_t sub, uint32_t nn, uint32_t (&q)[kChunk])
-{
-#pragma unroll
-    for (int c = 0; c < kChunk; ++c) {
-        const uint32_t k = sub + TPP * (j0 + c);
-        q[c] = (k < nn) ? __ldg(nl + (uint64_t)k * stride) : 0u;
-    }
-}
-
-// Sum v over the TPP threads of a particle group (lanes sub = 0..TPP-1 are
-// consecutive); every lane of the warp must call it.
-template <int TPP>
-__device__ __forceinline__ float group_sum(float v)
-{
-#pragma unroll
-    for (int o = TPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Visit the listed neighbours of one particle in list order, indices
-// prefetched CH at a time.
+// Visit list slots [0, nn) of one particle in list order (slot-major
+// layout: slot k of particle i at nl[k * stride], nl = nbr + i).  Indices are
+// requested CH at a time, one chunk ahead of their use; the chunk (loads in
+// flight against registers) is picked by the autotuner.  Whole chunks call f
+// without per-slot predicates; only the index requests and the final partial
+// chunk test k < nn.
 template <int CH, class F>
-__device__ __forceinline__ void for_list(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn, F &&f)
+__device__ __forceinline__ void list_walk(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn, F &&f)
 {
     uint32_t qn[CH];
-    prefetch_idx<CH>(nl, stride, 0, nn, qn);
-    for (uint32_t k0 = 0; k0 < nn; k0 += CH) {
+    const uint32_t *p = nl;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) qn[c] = ((uint32_t)c < nn) ? __ldg(p + c * stride) : 0u;
+    uint32_t k0 = 0;
+    for (; k0 + CH <= nn; k0 += CH) {
         uint32_t q[CH];
 #pragma unroll
         for (int c = 0; c < CH; ++c) q[c] = qn[c];
-        prefetch_idx<CH>(nl, stride, k0 + CH, nn, qn);
+        p += CH * stride;
 #pragma unroll
-        for (int c = 0; c < CH; ++c)
-            if (k0 + c < nn) f(q[c]);
+        for (int c = 0; c < CH; ++c) qn[c] = (k0 + CH + c < nn) ? __ldg(p + c * stride) : 0u;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) f(q[c]);
     }
+#pragma unroll
+    for (int c = 0; c < CH - 1; ++c)
+        if (k0 + c < nn) f(qn[c]);
 }
 
 // Per-tile prologue shared by the particle kernels.
@@ -564,19 +540,24 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
     // different candidates, so pair math inside the walk would run masked
     // for almost every candidate)
     uint32_t cnt = 0;
+    uint32_t *slot = nl;
     walk27_pruned(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
         if (dist2_exact(xp, __ldg(xa + q)) < h2) {
-            nl[(uint64_t)cnt * stride] = q;
+            *slot = q;
+            slot += stride;
             ++cnt;
         }
         return cnt < cap;
     });
     a.nnb[i] = (uint8_t)cnt;
-    // phase 2: lambda over the list just written (L2-resident)
+    // phase 2: lambda over the list just written (L2-resident; plain loads,
+    // the read-only path may not see this kernel's own stores)
     float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+    const uint32_t *rd = nl;
 #pragma unroll 4
     for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t q = nl[(uint64_t)k * stride];
+        const uint32_t q = *rd;
+        rd += stride;
         const PairK pk = pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta);
         ks += pk.W;
         g0 += pk.gx;
@@ -592,66 +573,72 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
 
 // lambda for iterations >= 1 (memorizeKernelCalc + calcScalingFactor,
 // pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
-// per-pair cache: W and grad W are recomputed from positions).
-// TPP threads share one particle (block = tile * TPP threads): thread `sub`
-// sums list slots sub, sub + TPP, ..., and the group adds its partial sums
-// with shuffles, so each particle has TPP independent chains of loads in
-// flight.  No thread leaves the tile loop early: the shuffles need the whole
-// warp.
-template <int kChunk, int TPP>
-__global__ void __launch_bounds__(1024) k_lambda(StepArgs a, const float4 *__restrict__ xc)
+// per-pair cache: W and grad W are recomputed from positions).  One thread
+// per particle; the neighbour sums run in list order.
+template <int kChunk>
+__global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, const float4 *__restrict__ xc)
 {
-    const uint32_t n_tiles = a.ctrl->n_tiles;
-    const uint32_t sub = threadIdx.x % TPP;
-    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const uint32_t s = __ldg(a.tile_scene + t);
-        const uint32_t local = __ldg(a.tile_start + t) + threadIdx.x / TPP;
-        const SceneDesc d = a.scenes[s];
-        const uint32_t base = a.offsets[d.c_off];
-        const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
-        const bool active = local < live;
-        const uint32_t i = d.p_off + (active ? local : 0u);
-        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-        const float4 xp = active ? xc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const uint32_t nn = active ? a.nnb[i] : 0u;
-        const uint64_t stride = a.nbr_stride;
-        const uint32_t *nl = a.nbr + i;
-        float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-        // chunks of kChunk of this thread's slots: the next chunk's indices
-        // are requested before this chunk's positions
-        uint32_t qn[kChunk];
-        prefetch_idx_sub<kChunk, TPP>(nl, stride, 0, sub, nn, qn);
-        for (uint32_t j0 = 0; sub + TPP * j0 < nn; j0 += kChunk) {
-            uint32_t q[kChunk];
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
-            prefetch_idx_sub<kChunk, TPP>(nl, stride, j0 + kChunk, sub, nn, qn);
-            float4 xq[kChunk];
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) xq[c] = (sub + TPP * (j0 + c) < nn) ? __ldg(xc + q[c]) : xp;
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) {
-                if (sub + TPP * (j0 + c) < nn) {
-                    const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
-                    ks += pk.W;
-                    g0 += pk.gx;
-                    g1 += pk.gy;
-                    g2 += pk.gz;
-                    kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
-                }
-            }
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const float4 xp = xc[i];
+    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
+        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
+        ks += pk.W;
+        g0 += pk.gx;
+        g1 += pk.gy;
+        g2 += pk.gz;
+        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+    });
+    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
+    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    TILE_LOOP_END
+}
+
+// s_corr forms, selected once per tile (a tile belongs to one scene).
+enum ScorrForm { kScorrReference, kScorrTextbook, kScorrOff, kScorrTextbook4 };
+
+// Sum over the list of -(lambda_i + lambda_j + s_corr) grad W (the body of
+// calcPositionUpdateCUDA, pbf_position_update.cu:131-188).
+template <int kChunk, int FORM>
+__device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, const float4 *__restrict__ xc,
+                                         uint32_t i, float4 xp, float li)
+{
+    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const float sci = (li < 0.f) ? -li : 0.f;
+    const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
+    const int sn = d.scorr_n;
+    const float *__restrict__ lam = a.lam;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
+        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
+        const float lj = __ldg(lam + q);
+        float corr = 0.f;
+        if (FORM == kScorrReference) {
+            const float kr2 = pk.W * pk.W;
+            const float tc = 10.f * (kr2 * kr2) * inv_k;
+            corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
+        } else if (FORM == kScorrTextbook4) {  // the loop below for n = 4, same products in the same order
+            const float ratio = pk.W * inv_wdq;
+            corr = sk * (((ratio * ratio) * ratio) * ratio);
+        } else if (FORM == kScorrTextbook) {
+            const float ratio = pk.W * inv_wdq;
+            float pw = 1.f;
+            for (int e = 0; e < sn; ++e) pw *= ratio;
+            corr = sk * pw;
         }
-        ks = group_sum<TPP>(ks);
-        g0 = group_sum<TPP>(g0);
-        g1 = group_sum<TPP>(g1);
-        g2 = group_sum<TPP>(g2);
-        kg2 = group_sum<TPP>(kg2);
-        if (active && sub == 0) {
-            const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
-            const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-            a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
-        }
-    }
+        const float cc = -(li + lj + corr);
+        s0 += cc * pk.gx;
+        s1 += cc * pk.gy;
+        s2 += cc * pk.gz;
+    });
+    return make_float3(s0, s1, s2);
 }
 
 // delta-p with s_corr (calcPositionUpdateCUDA cached, pbf_position_update.cu:131-188),
@@ -660,87 +647,38 @@ __global__ void __launch_bounds__(1024) k_lambda(StepArgs a, const float4 *__res
 // buffer so neighbours still read the old positions.  On the last iteration
 // the velocity update (updateVelocityCUDA, pbf_update.cu:25-39) is fused in:
 // v = (x_new - x_old) / dt, written with x_new to the particle phase.
-template <int kChunk, int TPP>
-__global__ void __launch_bounds__(1024) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
-                                           float4 *__restrict__ vo, int last)
+template <int kChunk>
+__global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
+                                               float4 *__restrict__ vo, int last)
 {
-    const uint32_t n_tiles = a.ctrl->n_tiles;
-    const uint32_t sub = threadIdx.x % TPP;
-    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const uint32_t s = __ldg(a.tile_scene + t);
-        const uint32_t local = __ldg(a.tile_start + t) + threadIdx.x / TPP;
-        const SceneDesc d = a.scenes[s];
-        const uint32_t base = a.offsets[d.c_off];
-        const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
-        if (last && local == 0 && sub == 0) a.scene_num[s] = live;
-        const bool active = local < live;
-        const uint32_t i = d.p_off + (active ? local : 0u);
-        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-        const float4 xp = active ? xc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float li = active ? a.lam[i] : 0.f;
-        const float sci = (li < 0.f) ? -li : 0.f;
-        const int mode = d.tensile_mode;
-        const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
-        const int sn = d.scorr_n;
-        const uint32_t nn = active ? a.nnb[i] : 0u;
-        const uint64_t stride = a.nbr_stride;
-        const uint32_t *nl = a.nbr + i;
-        const float *__restrict__ lam = a.lam;
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-        uint32_t qn[kChunk];
-        prefetch_idx_sub<kChunk, TPP>(nl, stride, 0, sub, nn, qn);
-        for (uint32_t j0 = 0; sub + TPP * j0 < nn; j0 += kChunk) {
-            uint32_t q[kChunk];
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) q[c] = qn[c];
-            prefetch_idx_sub<kChunk, TPP>(nl, stride, j0 + kChunk, sub, nn, qn);
-            float4 xq[kChunk];
-            float lq[kChunk];
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) {
-                const bool ok = sub + TPP * (j0 + c) < nn;
-                xq[c] = ok ? __ldg(xc + q[c]) : xp;
-                lq[c] = ok ? __ldg(lam + q[c]) : 0.f;
-            }
-#pragma unroll
-            for (int c = 0; c < kChunk; ++c) {
-                if (sub + TPP * (j0 + c) < nn) {
-                    const PairK pk = pair_kernel(xp, xq[c], inv_h, alpha, beta);
-                    const float lj = lq[c];
-                    float corr = 0.f;
-                    if (mode == PBF_TENSILE_REFERENCE) {
-                        const float kr2 = pk.W * pk.W;
-                        const float tc = 10.f * (kr2 * kr2) * inv_k;
-                        corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
-                    } else if (mode == PBF_TENSILE_TEXTBOOK) {
-                        const float ratio = pk.W * inv_wdq;
-                        float pw = 1.f;
-                        for (int e = 0; e < sn; ++e) pw *= ratio;
-                        corr = sk * pw;
-                    }
-                    const float cc = -(li + lj + corr);
-                    s0 += cc * pk.gx;
-                    s1 += cc * pk.gy;
-                    s2 += cc * pk.gz;
-                }
-            }
-        }
-        s0 = group_sum<TPP>(s0);
-        s1 = group_sum<TPP>(s1);
-        s2 = group_sum<TPP>(s2);
-        if (active && sub == 0) {
-            float3 dp = make_float3(s0 * d.m * d.inv_rho0, s1 * d.m * d.inv_rho0, s2 * d.m * d.inv_rho0);
-            const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
-            if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
-            const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
-            xo[i] = xn;
-            if (last) {
-                const float4 xo_ = a.xold[i];
-                vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z),
-                                    0.f);
-            }
-        }
+    TILE_LOOP_BEGIN
+    const SceneDesc d = a.scenes[s];
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+    if (last && local == 0) a.scene_num[s] = live;
+    if (local >= live) continue;
+    const uint32_t i = d.p_off + local;
+    const float4 xp = xc[i];
+    const float li = a.lam[i];
+    float3 sum;
+    if (d.tensile_mode == PBF_TENSILE_REFERENCE)
+        sum = dp_sum<kChunk, kScorrReference>(a, d, xc, i, xp, li);
+    else if (d.tensile_mode == PBF_TENSILE_TEXTBOOK && d.scorr_n == 4)
+        sum = dp_sum<kChunk, kScorrTextbook4>(a, d, xc, i, xp, li);
+    else if (d.tensile_mode == PBF_TENSILE_TEXTBOOK)
+        sum = dp_sum<kChunk, kScorrTextbook>(a, d, xc, i, xp, li);
+    else
+        sum = dp_sum<kChunk, kScorrOff>(a, d, xc, i, xp, li);
+    float3 dp = make_float3(sum.x * d.m * d.inv_rho0, sum.y * d.m * d.inv_rho0, sum.z * d.m * d.inv_rho0);
+    const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
+    if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
+    const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
+    xo[i] = xn;
+    if (last) {
+        const float4 xo_ = a.xold[i];
+        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
     }
+    TILE_LOOP_END
 }
 
 // iters == 0: positions stay at the prediction; v from the velocity update.
@@ -761,24 +699,23 @@ __global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict
 }
 
 // Vorticity, pass 1 (calcVorticityCUDA, pbf_vorticity_confinement.cu:87-115):
-// omega_i = m/rho0 * sum_j (v_j - v_i) x r_hat * W'(r), uncapped 27-cell walk.
-// Mode REFERENCE passes h where 1/h is expected (pbf_vorticity_confinement.cu:28).
+// omega_i = m/rho0 * sum_j (v_j - v_i) x r_hat * W'(r).  REF: the reference's
+// uncapped 27-cell walk, with h passed where 1/h is expected
+// (pbf_vorticity_confinement.cu:28); otherwise the textbook kernel over the
+// step's neighbour list.  Each form is its own kernel (scenes of the other
+// forms are skipped) so the list form keeps a lean register allocation.
+template <bool REF>
 __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__restrict__ vs)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
+    if (d.vort_mode != (REF ? PBF_VORTICITY_REFERENCE : PBF_VORTICITY_TEXTBOOK)) continue;
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
-    if (d.vort_mode == PBF_VORTICITY_OFF) continue;
     const uint32_t i = d.p_off + local;
     const float4 xi = a.x[i], vi = vs[i];
-    const bool ref = d.vort_mode == PBF_VORTICITY_REFERENCE;
-    const float kh = ref ? d.h : d.inv_h;
-    // W'(r) = 0 beyond h for the textbook kernel, so those candidates add
-    // nothing; the reference form (kernel scaled by h, not 1/h) reaches the
-    // whole 27-cell block and is walked in full
-    const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
+    const float kh = REF ? d.h : d.inv_h;
     const float4 *__restrict__ x = a.x;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
     auto use = [&](uint32_t j) {
@@ -795,39 +732,39 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             w2 += (v0 * p1 - v1 * p0) * wd;
         }
     };
-    if (ref) {  // the reference's uncapped walk around the final position
+    if (REF) {  // the kernel scaled by h reaches the whole 27-cell block
         walk27_batched(
             d, a.offsets, d.p_off - base, xi,
             [&](uint32_t j) -> bool {
                 const float4 xj = __ldg(x + j);
                 const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-                const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-                return r2 > 0.f && r2 <= rcut2;
+                return p0 * p0 + p1 * p1 + p2 * p2 > 0.f;
             },
             use);
-    } else {  // textbook form over the step's neighbour list
-        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+    } else {
+        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
     }
     const float mr = d.m * d.inv_rho0;
-    a.w[i] = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
+    const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
+    // |omega| once per particle in .w: pass 2 needs it for every neighbour
+    a.w[i] = make_float4(wi.x, wi.y, wi.z, sqrtf(wi.x * wi.x + wi.y * wi.y + wi.z * wi.z));
     TILE_LOOP_END
 }
 
 // Vorticity, pass 2 (addVorticityConfinementCUDA, pbf_vorticity_confinement.cu:192-222).
+template <bool REF>
 __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restrict__ vs)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
+    if (d.vort_mode != (REF ? PBF_VORTICITY_REFERENCE : PBF_VORTICITY_TEXTBOOK)) continue;
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
-    if (d.vort_mode == PBF_VORTICITY_OFF) continue;
     const uint32_t i = d.p_off + local;
     const float4 xi = a.x[i];
-    const bool ref = d.vort_mode == PBF_VORTICITY_REFERENCE;
-    const float kh = ref ? d.h : d.inv_h;
-    const float sgn = ref ? 1.f : -1.f;
-    const float rcut2 = ref ? INFINITY : d.h2 * 1.0001f;
+    const float kh = REF ? d.h : d.inv_h;
+    const float sgn = REF ? 1.f : -1.f;
     const float4 *__restrict__ x = a.x;
     const float4 *__restrict__ w = a.w;
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
@@ -837,31 +774,29 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
         const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
         if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
-            const float4 wj = __ldg(w + j);
-            const float wl = sqrtf(wj.x * wj.x + wj.y * wj.y + wj.z * wj.z);
+            const float wl = __ldg(&w[j].w);  // |omega_j|, stored by pass 1
             const float f = sgn * wl * wspiky_d(r2 * inv_r, kh) * inv_r;
             n0 += f * p0;
             n1 += f * p1;
             n2 += f * p2;
         }
     };
-    if (ref) {
+    if (REF) {
         walk27_batched(
             d, a.offsets, d.p_off - base, xi,
             [&](uint32_t j) -> bool {
                 const float4 xj = __ldg(x + j);
                 const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-                const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
-                return r2 > 0.f && r2 <= rcut2;
+                return p0 * p0 + p1 * p1 + p2 * p2 > 0.f;
             },
             use);
     } else {
-        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
     }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
     float4 v = vs[i];
-    if (ref) {
+    if (REF) {
         if (sqrtf(n0 * n0 + n1 * n1 + n2 * n2) > 0.f) {
             n0 = n0 * d.m * d.inv_rho0;
             n1 = n1 * d.m * d.inv_rho0;
@@ -889,37 +824,46 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
 }
 
 // XSPH (calcXSPHCUDA, pbf_xsph.cu:84-113): v_i += c m/rho0 sum_j (v_j - v_i) W(r_ij),
-// uncapped 27-cell walk, NaN guard.
+// NaN guard.  WALK: the reference's uncapped 27-cell walk (scenes with
+// PBF_XSPH_WALK); otherwise over the step's neighbour list (scenes with
+// PBF_XSPH_LIST), also copying vs to vo for scenes without XSPH.
+template <bool WALK>
 __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restrict__ vs, float4 *__restrict__ vo)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
+    if ((d.xsph_mode == PBF_XSPH_WALK) != WALK) continue;
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
     const uint32_t i = d.p_off + local;
     const float4 xi = a.x[i], vi = vs[i];
-    if (d.xsph_mode == 0) {  // scene without XSPH in a batch that has some
+    if (!WALK && d.xsph_mode == PBF_XSPH_OFF) {  // scene without XSPH in a batch that has some
         vo[i] = vi;
         continue;
     }
     const float inv_h = d.inv_h, alpha6 = d.alpha6;
-    // W = 0 beyond h: those candidates add nothing (a non-finite velocity of
-    // a non-neighbour is no longer folded into the sum; such particles raise
-    // PBF_FLAG_NONFINITE in the next step's prediction)
-    const float rcut2 = d.h2 * 1.0001f;
     const float4 *__restrict__ x = a.x;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    const float ih2 = inv_h * inv_h;
     auto use = [&](uint32_t j) {
         const float4 xj = __ldg(x + j);
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
-        const float W = wpoly6(sqrtf(p0 * p0 + p1 * p1 + p2 * p2), inv_h, alpha6);
+        // Wpoly6 from r^2 (q^2 = r^2 / h^2 instead of (|r| / h)^2: no square
+        // root per pair; the two differ by rounding only)
+        const float q2 = (p0 * p0 + p1 * p1 + p2 * p2) * ih2;
+        const float t = 1.f - q2;
+        const float W = (q2 <= 1.f) ? alpha6 * t * t * t : 0.f;
         const float4 vj = __ldg(vs + j);
         s0 += (vj.x - vi.x) * W;
         s1 += (vj.y - vi.y) * W;
         s2 += (vj.z - vi.z) * W;
     };
-    if (d.xsph_mode == 1) {  // the reference's uncapped walk
+    if (WALK) {
+        // W = 0 beyond h: those candidates add nothing (a non-finite velocity
+        // of a non-neighbour is no longer folded into the sum; such particles
+        // raise PBF_FLAG_NONFINITE in the next step's prediction)
+        const float rcut2 = d.h2 * 1.0001f;
         walk27_batched(
             d, a.offsets, d.p_off - base, xi,
             [&](uint32_t j) -> bool {
@@ -928,8 +872,8 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
                 return p0 * p0 + p1 * p1 + p2 * p2 <= rcut2;
             },
             use);
-    } else {  // over the step's neighbour list
-        for_list<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+    } else {
+        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
     }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
@@ -999,35 +943,28 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 
 }  // namespace
 
-// The lambda / delta-p variants: neighbour chunk kChunk x threads per
-// particle TPP, selected at run time by (chunk, tpp).
-template <int CH, int TPP>
+// The lambda / delta-p variants by neighbour chunk, selected at run time.
+template <int CH>
 struct PassFns {
-    static const void *lambda() { return (const void *)k_lambda<CH, TPP>; }
-    static const void *dp() { return (const void *)k_dp<CH, TPP>; }
+    static const void *lambda() { return (const void *)k_lambda<CH>; }
+    static const void *dp() { return (const void *)k_dp<CH>; }
     static void launch_lambda(const StepArgs &a, const LaunchShape &sh, const float4 *cur, cudaStream_t st)
     {
-        k_lambda<CH, TPP><<<sh.grid_lambda, sh.tile * TPP, 0, st>>>(a, cur);
+        k_lambda<CH><<<sh.grid_lambda, sh.tile, 0, st>>>(a, cur);
     }
     static void launch_dp(const StepArgs &a, const LaunchShape &sh, const float4 *cur, float4 *out, float4 *vo,
                           int last, cudaStream_t st)
     {
-        k_dp<CH, TPP><<<sh.grid_dp, sh.tile * TPP, 0, st>>>(a, cur, out, vo, last);
+        k_dp<CH><<<sh.grid_dp, sh.tile, 0, st>>>(a, cur, out, vo, last);
     }
 };
 
-#define PBF_PASS_DISPATCH(chunk, tpp, CALL)       \
-    switch ((chunk) * 10 + (tpp)) {               \
-    case 41: PassFns<4, 1>::CALL; break;          \
-    case 42: PassFns<4, 2>::CALL; break;          \
-    case 44: PassFns<4, 4>::CALL; break;          \
-    case 81: PassFns<8, 1>::CALL; break;          \
-    case 82: PassFns<8, 2>::CALL; break;          \
-    default: PassFns<8, 4>::CALL; break;          \
-    }
+#define PBF_PASS_DISPATCH(chunk, CALL) \
+    if ((chunk) == 4) PassFns<4>::CALL; \
+    else PassFns<8>::CALL;
 
 // Resident blocks per SM for the heaviest tile kernels at this block size.
-Occupancy occupancy(uint32_t tile, uint32_t chunk, uint32_t tpp)
+Occupancy occupancy(uint32_t tile, uint32_t chunk)
 {
     auto occ_b = [](const void *fn, uint32_t block) -> uint32_t {
         int b = 0;
@@ -1040,18 +977,11 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk, uint32_t tpp)
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
                  mn(occ((const void *)k_rank_reorder), occ((const void *)k_finalize)));
     o.nb = occ((const void *)k_neighbors_lambda);
-    const void *fl = nullptr, *fd = nullptr;
-    switch (chunk * 10 + tpp) {
-    case 41: fl = PassFns<4, 1>::lambda(); fd = PassFns<4, 1>::dp(); break;
-    case 42: fl = PassFns<4, 2>::lambda(); fd = PassFns<4, 2>::dp(); break;
-    case 44: fl = PassFns<4, 4>::lambda(); fd = PassFns<4, 4>::dp(); break;
-    case 81: fl = PassFns<8, 1>::lambda(); fd = PassFns<8, 1>::dp(); break;
-    case 82: fl = PassFns<8, 2>::lambda(); fd = PassFns<8, 2>::dp(); break;
-    default: fl = PassFns<8, 4>::lambda(); fd = PassFns<8, 4>::dp(); break;
-    }
-    o.lambda = occ_b(fl, tile * tpp);
-    o.dp = occ_b(fd, tile * tpp);
-    o.list = mn(mn(occ((const void *)k_vort_omega), occ((const void *)k_vort_apply)), occ((const void *)k_xsph));
+    const bool c4 = chunk == 4;
+    o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
+    o.dp = occ(c4 ? PassFns<4>::dp() : PassFns<8>::dp());
+    o.list = mn(mn(occ((const void *)k_vort_omega<false>), occ((const void *)k_vort_apply<false>)),
+                occ((const void *)k_xsph<false>));
     return o;
 }
 
@@ -1079,7 +1009,7 @@ void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_
     k_pack<<<sh.grid, sh.tile, 0, st>>>(a, pack_off, dst_x, dst_v);
 }
 
-uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool xsph, bool vort,
+uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint32_t post,
                       cudaStream_t st, StepHook *hook)
 {
     uint32_t nl = 0;
@@ -1103,16 +1033,17 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
     PBF_LAUNCHED("k_rank_reorder");
     k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
     PBF_LAUNCHED("k_neighbors_lambda");
+    const bool xsph = (post & (kPostXsphWalk | kPostXsphList)) != 0;
     float4 *vfinal = xsph ? a.vt : a.v;
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            PBF_PASS_DISPATCH(sh.chunk, sh.tpp, launch_lambda(a, sh, cur, st));
+            PBF_PASS_DISPATCH(sh.chunk, launch_lambda(a, sh, cur, st));
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        PBF_PASS_DISPATCH(sh.chunk, sh.tpp, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
+        PBF_PASS_DISPATCH(sh.chunk, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;
@@ -1122,15 +1053,31 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, bool 
         k_finalize<<<g, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_finalize");
     }
-    if (vort) {
-        k_vort_omega<<<sh.grid_list, b, 0, st>>>(a, vfinal);
+    // omega of every form before any apply: both forms read final positions
+    // and velocities only
+    if (post & kPostVortTextbook) {
+        k_vort_omega<false><<<sh.grid_list, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega");
-        k_vort_apply<<<sh.grid_list, b, 0, st>>>(a, vfinal);
+    }
+    if (post & kPostVortReference) {
+        k_vort_omega<true><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        PBF_LAUNCHED("k_vort_omega_walk");
+    }
+    if (post & kPostVortTextbook) {
+        k_vort_apply<false><<<sh.grid_list, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply");
     }
-    if (xsph) {
-        k_xsph<<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
+    if (post & kPostVortReference) {
+        k_vort_apply<true><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        PBF_LAUNCHED("k_vort_apply_walk");
+    }
+    if (post & kPostXsphList) {
+        k_xsph<false><<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph");
+    }
+    if (post & kPostXsphWalk) {
+        k_xsph<true><<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
+        PBF_LAUNCHED("k_xsph_walk");
     }
 #undef PBF_LAUNCHED
     return nl;
