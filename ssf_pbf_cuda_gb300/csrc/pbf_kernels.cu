@@ -79,17 +79,7 @@ __device__ __forceinline__ PairK pair_kernel(float4 xi, float4 xj, float inv_h, 
     return o;
 }
 
-// Wpoly6 / WspikyDerivative, src/pbf/kernel/cuda/detail/pbf_kernel.inl:34-63.
-__device__ __forceinline__ float wpoly6(float r, float inv_h, float alpha6)
-{
-    const float q = r * inv_h;
-    if (q <= 1.f) {
-        const float t = 1.f - q * q;
-        return alpha6 * t * t * t;
-    }
-    return 0.f;
-}
-
+// WspikyDerivative, src/pbf/kernel/cuda/detail/pbf_kernel.inl:48-63.
 __device__ __forceinline__ float wspiky_d(float r, float kinv_h)
 {
     const float q = r * kinv_h;
@@ -183,91 +173,66 @@ __device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, floa
 
 // Visit the particles of the 27 cells around xp in the reference's order
 // (z, y, x from -1 to 1; ascending sorted index inside a cell,
-// pbf_neighbor_search_util.cu:428-452).  When the three x-cells of a row are
-// consecutive hashes their particles form one contiguous sorted range, which
-// is walked as one loop.  f(q) returns false to stop the walk.
-template <class F>
-__device__ __forceinline__ void walk27(const SceneDesc &d, const uint32_t *__restrict__ offsets, uint32_t shift,
-                                       float4 xp, F &&f)
-{
-    const uint32_t gx = (uint32_t)cell_coord(xp.x, d.cw);
-    const uint32_t gy = (uint32_t)cell_coord(xp.y, d.cw);
-    const uint32_t gz = (uint32_t)cell_coord(xp.z, d.cw);
-    const uint32_t *off = offsets + d.c_off;
-    const uint32_t mx = d.gx - 1u;
-    const uint32_t x0c = (gx - 1u) & mx, x2c = (gx + 1u) & mx;
-    const bool contiguous = (x2c == x0c + 2u);
-    for (int dz = -1; dz <= 1; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
-                                 ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
-            if (contiguous) {
-                const uint32_t st = __ldg(off + row + x0c) + shift;
-                const uint32_t en = __ldg(off + row + x2c + 1u) + shift;
-                for (uint32_t q = st; q != en; ++q)
-                    if (!f(q)) return;
-            } else {
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const uint32_t xc = (gx + (uint32_t)dx) & mx;
-                    const uint32_t st = __ldg(off + row + xc) + shift;
-                    const uint32_t en = __ldg(off + row + xc + 1u) + shift;
-                    for (uint32_t q = st; q != en; ++q)
-                        if (!f(q)) return;
-                }
-            }
-        }
-    }
-}
-
-// walk27 restricted to cells that can hold a particle within h of xp (the
-// binned position): a cell, or a whole row of three, whose nearest point is
-// farther than h holds no accepted candidate, so skipping it leaves the
+// pbf_neighbor_search_util.cu:428-452), as contiguous sorted-index ranges:
+// r(st, en) gets [st, en) and returns false to stop the walk.  When the
+// three x-cells of a row are consecutive hashes their particles form one
+// range.
+//
+// PRUNE restricts the walk to cells that can hold a particle within h of xp
+// (the binned position): a cell, or a whole row of three, whose nearest point
+// is farther than h holds no accepted candidate, so skipping it leaves the
 // visited sequence of accepted candidates unchanged.  A 1e-3 relative margin
 // covers the rounding of the cell assignment.  With fewer than 4 cells on an
-// axis the reference visits wrapped cells more than once; then the full walk
-// runs.
-template <class F>
-__device__ __forceinline__ void walk27_pruned(const SceneDesc &d, const uint32_t *__restrict__ offsets,
-                                              uint32_t shift, float4 xp, F &&f)
+// axis the reference visits wrapped cells more than once; then every cell is
+// visited.  The rows and cells are one loop nest with a single call site of
+// r, so r's body is inlined once.
+template <bool PRUNE, class R>
+__device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t *__restrict__ offsets,
+                                              uint32_t shift, float4 xp, R &&r)
 {
-    if (d.gx < 4 || d.gy < 4 || d.gz < 4) {
-        walk27(d, offsets, shift, xp, f);
-        return;
-    }
     const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
-    const float lx = xp.x - (float)icx * d.cw, ly = xp.y - (float)icy * d.cw, lz = xp.z - (float)icz * d.cw;
-    const float rx = d.cw - lx, ry = d.cw - ly, rz = d.cw - lz;
+    const bool prune = PRUNE && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+    float lx = 0.f, ly = 0.f, lz = 0.f, rx = 0.f, ry = 0.f, rz = 0.f;
+    if (prune) {
+        lx = xp.x - (float)icx * d.cw;
+        ly = xp.y - (float)icy * d.cw;
+        lz = xp.z - (float)icz * d.cw;
+        rx = d.cw - lx;
+        ry = d.cw - ly;
+        rz = d.cw - lz;
+    }
     const float lim = d.h2 * 1.001f;
     const uint32_t gx = (uint32_t)icx, gy = (uint32_t)icy, gz = (uint32_t)icz;
     const uint32_t *off = offsets + d.c_off;
     const uint32_t mx = d.gx - 1u;
     const uint32_t x0c = (gx - 1u) & mx, x1c = gx & mx, x2c = (gx + 1u) & mx;
     const bool contiguous = (x2c == x0c + 2u);
-    for (int dz = -1; dz <= 1; ++dz) {
-        const float ez = dz < 0 ? lz : (dz > 0 ? rz : 0.f);
-        for (int dy = -1; dy <= 1; ++dy) {
+#pragma unroll 1
+    for (int rr = 0; rr < 9; ++rr) {
+        const int dz = rr / 3 - 1, dy = rr % 3 - 1;
+        bool left = true, right = true;
+        if (prune) {
+            const float ez = dz < 0 ? lz : (dz > 0 ? rz : 0.f);
             const float ey = dy < 0 ? ly : (dy > 0 ? ry : 0.f);
             const float eyz2 = ey * ey + ez * ez;
             if (eyz2 > lim) continue;
-            const bool left = eyz2 + lx * lx <= lim, right = eyz2 + rx * rx <= lim;
-            const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
-                                 ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
+            left = eyz2 + lx * lx <= lim;
+            right = eyz2 + rx * rx <= lim;
+        }
+        const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
+                             ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
+        const uint32_t nseg = contiguous ? 1u : 3u;
+#pragma unroll 1
+        for (uint32_t sg = 0; sg < nseg; ++sg) {
+            uint32_t lo, hi;
             if (contiguous) {
-                const uint32_t first = left ? x0c : x1c, last = right ? x2c : x1c;
-                const uint32_t st = __ldg(off + row + first) + shift;
-                const uint32_t en = __ldg(off + row + last + 1u) + shift;
-                for (uint32_t q = st; q != en; ++q)
-                    if (!f(q)) return;
+                lo = left ? x0c : x1c;
+                hi = right ? x2c : x1c;
             } else {
-                for (int dx = -1; dx <= 1; ++dx) {
-                    if ((dx < 0 && !left) || (dx > 0 && !right)) continue;
-                    const uint32_t xc = (gx + (uint32_t)dx) & mx;
-                    const uint32_t st = __ldg(off + row + xc) + shift;
-                    const uint32_t en = __ldg(off + row + xc + 1u) + shift;
-                    for (uint32_t q = st; q != en; ++q)
-                        if (!f(q)) return;
-                }
+                if ((sg == 0 && !left) || (sg == 2 && !right)) continue;
+                lo = hi = (gx + sg - 1u) & mx;
             }
+            if (!r(__ldg(off + row + lo) + shift, __ldg(off + row + hi + 1u) + shift)) return;
         }
     }
 }
@@ -283,12 +248,14 @@ __device__ __forceinline__ void walk27_batched(const SceneDesc &d, const uint32_
     constexpr int kBuf = 32;
     uint32_t buf[kBuf];
     int nb = 0;
-    walk27(d, offsets, shift, xp, [&](uint32_t j) -> bool {
-        if (accept(j)) {
-            buf[nb++] = j;
-            if (nb == kBuf) {
-                for (int k = 0; k < kBuf; ++k) use(buf[k]);
-                nb = 0;
+    walk27_ranges<false>(d, offsets, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
+        for (uint32_t j = st; j < en; ++j) {
+            if (accept(j)) {
+                buf[nb++] = j;
+                if (nb == kBuf) {
+                    for (int k = 0; k < kBuf; ++k) use(buf[k]);
+                    nb = 0;
+                }
             }
         }
         return true;
@@ -521,7 +488,7 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
 // (calcScalingFactorCUDA cached, pbf_constraint.cu:168-209): at iteration 0
 // the working positions are the sorted predicted positions, so the pair
 // terms can be summed while the list is built.
-__global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
+__global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
@@ -539,15 +506,27 @@ __global__ void __launch_bounds__(512) k_neighbors_lambda(StepArgs a)
     // phase 1: the walk only tests and records (lanes of a warp accept
     // different candidates, so pair math inside the walk would run masked
     // for almost every candidate)
+    // Candidates are fetched kNbFetch at a time (more loads in flight) and
+    // tested in order, so the first `cap` accepted ones are the reference's.
+    constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
     uint32_t *slot = nl;
-    walk27_pruned(d, a.offsets, shift, xp, [&](uint32_t q) -> bool {
-        if (dist2_exact(xp, __ldg(xa + q)) < h2) {
-            *slot = q;
-            slot += stride;
-            ++cnt;
+    walk27_ranges<true>(d, a.offsets, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
+        for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
+            float4 c[kNbFetch];
+#pragma unroll
+            for (uint32_t k = 0; k < kNbFetch; ++k)
+                if (q0 + k < en) c[k] = __ldg(xa + q0 + k);
+#pragma unroll
+            for (uint32_t k = 0; k < kNbFetch; ++k) {
+                if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
+                    *slot = q0 + k;
+                    slot += stride;
+                    if (++cnt == cap) return false;
+                }
+            }
         }
-        return cnt < cap;
+        return true;
     });
     a.nnb[i] = (uint8_t)cnt;
     // phase 2: lambda over the list just written (L2-resident; plain loads,
