@@ -616,7 +616,9 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.grid_nb = g(o.nb);
     sh.grid_lambda = g(o.lambda);
     sh.grid_dp = g(o.dp);
-    sh.grid_list = g(o.list);
+    sh.grid_omega = g(o.omega);
+    sh.grid_apply = g(o.apply);
+    sh.grid_xsph = g(o.xsph);
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     return sh;

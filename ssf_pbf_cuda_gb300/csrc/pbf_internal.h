@@ -88,18 +88,18 @@ struct LaunchShape {
     uint32_t scan_grid;   // grid for the scan kernels
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
     // persistent grids of the heavy kernels, each from its own occupancy
-    uint32_t grid_nb, grid_lambda, grid_dp, grid_list;
+    uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
-               grid_list == o.grid_list;
+               grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
 };
 
 // Resident blocks per SM of each kernel class at a tile size / chunk.
 struct Occupancy {
-    uint32_t light, nb, lambda, dp, list;
+    uint32_t light, nb, lambda, dp, omega, apply, xsph;
 };
 Occupancy occupancy(uint32_t tile, uint32_t chunk);
 

@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             },
             use);
     } else {
-        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<8>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
     }
     const float mr = d.m * d.inv_rho0;
     const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
@@ -770,7 +770,7 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             },
             use);
     } else {
-        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);  // 4: fewer registers, more warps (measured)
     }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
@@ -852,7 +852,7 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
             },
             use);
     } else {
-        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<8>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
     }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
@@ -959,8 +959,9 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
     o.dp = occ(c4 ? PassFns<4>::dp() : PassFns<8>::dp());
-    o.list = mn(mn(occ((const void *)k_vort_omega<false>), occ((const void *)k_vort_apply<false>)),
-                occ((const void *)k_xsph<false>));
+    o.omega = occ((const void *)k_vort_omega<false>);
+    o.apply = occ((const void *)k_vort_apply<false>);
+    o.xsph = occ((const void *)k_xsph<false>);
     return o;
 }
 
@@ -1035,27 +1036,27 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     // omega of every form before any apply: both forms read final positions
     // and velocities only
     if (post & kPostVortTextbook) {
-        k_vort_omega<false><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        k_vort_omega<false><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega");
     }
     if (post & kPostVortReference) {
-        k_vort_omega<true><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        k_vort_omega<true><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega_walk");
     }
     if (post & kPostVortTextbook) {
-        k_vort_apply<false><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        k_vort_apply<false><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply");
     }
     if (post & kPostVortReference) {
-        k_vort_apply<true><<<sh.grid_list, b, 0, st>>>(a, vfinal);
+        k_vort_apply<true><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply_walk");
     }
     if (post & kPostXsphList) {
-        k_xsph<false><<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
+        k_xsph<false><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph");
     }
     if (post & kPostXsphWalk) {
-        k_xsph<true><<<sh.grid_list, b, 0, st>>>(a, a.vt, a.v);
+        k_xsph<true><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph_walk");
     }
 #undef PBF_LAUNCHED
