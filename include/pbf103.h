@@ -67,6 +67,9 @@ typedef enum pbf_status {
 #define PBF_FLAG_COLLISION_LIMIT 0x2u  /* a particle hit max_collision_passes
                                           (the reference loops without bound,
                                           pbf_response_collision.cu:33) */
+#define PBF_FLAG_CAPACITY 0x4u         /* a device-side append (pbf_generate,
+                                          pbf_emit) did not fit the capacity
+                                          and added nothing */
 
 /* s_corr (tensile instability) forms */
 #define PBF_TENSILE_REFERENCE 0  /* 10 W^4 / W(0.4h)^4 * (max(-l_i,0)+max(-l_j,0)),
@@ -255,6 +258,75 @@ pbf_status pbf_batch_profile_step(pbf_batch *b, int iters, void *stream, float *
 pbf_status pbf_profile_step(pbf_handle *h, const pbf_boundary_t *boundary, const float area_min[3],
                             const float area_max[3], int iters, void *stream, float *ms, char *names, uint32_t max,
                             uint32_t *n);
+
+/* ---- particle sets: ids, order restore, generators, emitters ----
+ *
+ * Every particle carries a 32-bit id that follows it through the per-step
+ * sort.  pbf_set_particles numbers the particles 0..n-1; pbf_add_particles,
+ * pbf_generate and pbf_emit continue from the scene's counter. */
+
+/* Ids of the num particles in their current (sorted) order. */
+pbf_status pbf_get_particle_ids(pbf_handle *h, uint32_t *ids, int dst_is_device, void *stream);
+/* restoreOrder (src/pbf/interaction/cuda/pbf_neighbor_search_util.cu:156-170,
+ * 344-359): x_out[perm[i]] = x[i] for the live particles, i.e. the order of
+ * the last step's input.  n_out bounds the output (entries >= n_out and
+ * those of deleted particles are left as they were).  Needs a step since
+ * the last change of the particle set (else PBF_ERROR_NOT_READY). */
+pbf_status pbf_restore_order(pbf_handle *h, float *x, float *v, uint32_t n_out, int dst_is_device, void *stream);
+/* x_out[id] = x of the particle with that id, for ids < n_out (no reference
+ * counterpart: the input order of the first step, across any number of steps). */
+pbf_status pbf_get_particles_by_id(pbf_handle *h, float *x, float *v, uint32_t n_out, int dst_is_device,
+                                   void *stream);
+
+/* The reference's arrangement generators (src/pbf/util/pbf_arrangement.h),
+ * evaluated on the device. */
+#define PBF_ARRANGE_VOLUME 0     /* cartesian_volume(origin, end, space), :82-99 */
+#define PBF_ARRANGE_RECTANGLE 1  /* cartesian_rectangle(axis, axis_value, origin2, end2, space), :123-163 */
+#define PBF_ARRANGE_LINE 2       /* cartesian_line_inclusive(origin, end, space), :8-18 */
+#define PBF_ARRANGE_CYLINDER 3   /* cartesian_cylinder(axis, axis_value, origin2, radius, height, space), :212-244 */
+typedef struct pbf_arrangement {
+    int32_t kind;        /* PBF_ARRANGE_* */
+    int32_t axis;        /* rectangle / cylinder: 0 = "x", 1 = "y", 2 = "z" */
+    float origin[3];     /* volume / line: 3-D; rectangle / cylinder: origin[0..1] is the 2-D origin */
+    float end[3];        /* volume / line: 3-D; rectangle: end[0..1] is the 2-D end */
+    float axis_value;    /* rectangle / cylinder */
+    float radius;        /* cylinder */
+    float height;        /* cylinder */
+    float space;         /* particle spacing */
+} pbf_arrangement;
+
+/* Points an arrangement generates (host arithmetic, as the reference's loops). */
+pbf_status pbf_arrangement_count(const pbf_arrangement *a, uint32_t *n);
+/* Append the arrangement's points with velocity v0 on the device, after the
+ * live particles, without a host round trip; if they do not fit the
+ * capacity nothing is added and PBF_FLAG_CAPACITY is raised.  *n_points
+ * (optional) receives the arrangement's point count. */
+pbf_status pbf_generate(pbf_handle *h, const pbf_arrangement *a, const float v0[3], void *stream,
+                        uint32_t *n_points);
+
+/* Emitter: a fixed set of positions and velocities resident on a device
+ * (the sphere scene's jet, src/simulator/sphere/pbf_sphere_sim.cpp:20-82). */
+typedef struct pbf_emitter pbf_emitter;
+pbf_status pbf_emitter_create(int device, const float *x, const float *v, uint32_t n, int src_is_device,
+                              pbf_emitter **out);
+pbf_status pbf_emitter_create_arrangement(int device, const pbf_arrangement *a, const float v0[3],
+                                          pbf_emitter **out);
+pbf_status pbf_emitter_size(const pbf_emitter *e, uint32_t *n);
+pbf_status pbf_emitter_destroy(pbf_emitter *e);
+/* Append the emitter's particles iff num < max_fill * capacity (the jet's
+ * rule, pbf_sphere_sim.cpp:386-387) and they fit; decided on the device. */
+pbf_status pbf_emit(pbf_handle *h, const pbf_emitter *e, double max_fill, void *stream);
+
+/* The same for one scene of a batch. */
+pbf_status pbf_batch_get_particle_ids(pbf_batch *b, uint32_t scene_id, uint32_t *ids, uint32_t *num,
+                                      int dst_is_device, void *stream);
+pbf_status pbf_batch_restore_order(pbf_batch *b, uint32_t scene_id, float *x, float *v, uint32_t n_out,
+                                   int dst_is_device, void *stream);
+pbf_status pbf_batch_get_particles_by_id(pbf_batch *b, uint32_t scene_id, float *x, float *v, uint32_t n_out,
+                                         int dst_is_device, void *stream);
+pbf_status pbf_batch_generate(pbf_batch *b, uint32_t scene_id, const pbf_arrangement *a, const float v0[3],
+                              void *stream, uint32_t *n_points);
+pbf_status pbf_batch_emit(pbf_batch *b, uint32_t scene_id, const pbf_emitter *e, double max_fill, void *stream);
 
 /* ---- continuous-batching server ---- */
 typedef struct pbf_server_config {

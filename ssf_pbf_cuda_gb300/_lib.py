@@ -25,6 +25,8 @@ STATUS_NAMES = {
 }
 PBF_FLAG_NONFINITE = 0x1
 PBF_FLAG_COLLISION_LIMIT = 0x2
+PBF_FLAG_CAPACITY = 0x4
+PBF_ARRANGE_VOLUME, PBF_ARRANGE_RECTANGLE, PBF_ARRANGE_LINE, PBF_ARRANGE_CYLINDER = 0, 1, 2, 3
 PBF_TENSILE_REFERENCE, PBF_TENSILE_TEXTBOOK, PBF_TENSILE_OFF = 0, 1, 2
 PBF_VORTICITY_OFF, PBF_VORTICITY_REFERENCE, PBF_VORTICITY_TEXTBOOK = 0, 1, 2
 PBF_XSPH_OFF, PBF_XSPH_WALK, PBF_XSPH_LIST = 0, 1, 2
@@ -38,6 +40,13 @@ class PbfParams(ctypes.Structure):
         ("max_pair_particle_num", c_u32), ("tensile_mode", c_i32), ("scorr_k", c_f),
         ("scorr_n", c_i32), ("scorr_dq", c_f), ("xsph_mode", c_i32), ("vorticity_mode", c_i32),
         ("max_collision_passes", c_u32), ("cell_width", c_f), ("grid_size", c_u32 * 3),
+    ]
+
+
+class PbfArrangement(ctypes.Structure):
+    _fields_ = [
+        ("kind", c_i32), ("axis", c_i32), ("origin", c_f * 3), ("end", c_f * 3), ("axis_value", c_f),
+        ("radius", c_f), ("height", c_f), ("space", c_f),
     ]
 
 
@@ -118,6 +127,21 @@ SIGNATURES = {
     "pbf_batch_get_launch_shape": (c_i32, [c_vp, c_vp, c_vp]),
     "pbf_batch_set_graph_mode": (c_i32, [c_vp, ctypes.c_int]),
     "pbf_batch_last_launches": (c_i32, [c_vp, P(c_u32)]),
+    "pbf_get_particle_ids": (c_i32, [c_vp, c_vp, ctypes.c_int, c_vp]),
+    "pbf_restore_order": (c_i32, [c_vp, c_vp, c_vp, c_u32, ctypes.c_int, c_vp]),
+    "pbf_get_particles_by_id": (c_i32, [c_vp, c_vp, c_vp, c_u32, ctypes.c_int, c_vp]),
+    "pbf_arrangement_count": (c_i32, [P(PbfArrangement), P(c_u32)]),
+    "pbf_generate": (c_i32, [c_vp, P(PbfArrangement), P(c_f), c_vp, P(c_u32)]),
+    "pbf_emitter_create": (c_i32, [ctypes.c_int, c_vp, c_vp, c_u32, ctypes.c_int, P(c_vp)]),
+    "pbf_emitter_create_arrangement": (c_i32, [ctypes.c_int, P(PbfArrangement), P(c_f), P(c_vp)]),
+    "pbf_emitter_size": (c_i32, [c_vp, P(c_u32)]),
+    "pbf_emitter_destroy": (c_i32, [c_vp]),
+    "pbf_emit": (c_i32, [c_vp, c_vp, ctypes.c_double, c_vp]),
+    "pbf_batch_get_particle_ids": (c_i32, [c_vp, c_u32, c_vp, P(c_u32), ctypes.c_int, c_vp]),
+    "pbf_batch_restore_order": (c_i32, [c_vp, c_u32, c_vp, c_vp, c_u32, ctypes.c_int, c_vp]),
+    "pbf_batch_get_particles_by_id": (c_i32, [c_vp, c_u32, c_vp, c_vp, c_u32, ctypes.c_int, c_vp]),
+    "pbf_batch_generate": (c_i32, [c_vp, c_u32, P(PbfArrangement), P(c_f), c_vp, P(c_u32)]),
+    "pbf_batch_emit": (c_i32, [c_vp, c_u32, c_vp, ctypes.c_double, c_vp]),
     "pbf_server_create": (c_i32, [P(PbfServerConfig), P(c_vp)]),
     "pbf_server_destroy": (c_i32, [c_vp]),
     "pbf_server_submit": (c_i32, [c_vp, P(PbfRequestDesc), c_vp, c_vp, c_u32, P(c_u64)]),

@@ -13,7 +13,8 @@ import ctypes
 import numpy as np
 
 from . import _lib as L
-from ._lib import PbfParams, check, load
+from ._lib import (PBF_ARRANGE_CYLINDER, PBF_ARRANGE_LINE, PBF_ARRANGE_RECTANGLE, PBF_ARRANGE_VOLUME, PbfArrangement,
+                   PbfParams, check, load)
 
 _PARAM_KEYS = [f[0] for f in PbfParams._fields_]
 
@@ -111,6 +112,80 @@ def _ptr(a):
     if _is_device(a):
         return a.data_ptr()
     return a.ctypes.data
+
+
+_AXES = {"x": 0, "y": 1, "z": 2}
+
+
+def arrangement(kind: str, *, origin=(0.0, 0.0, 0.0), end=(0.0, 0.0, 0.0), space: float, axis: str = "x",
+                axis_value: float = 0.0, radius: float = 0.0, height: float = 0.0) -> PbfArrangement:
+    """The reference's arrangement generators (src/pbf/util/pbf_arrangement.h):
+    kind "volume" (cartesian_volume(origin, end, space)), "rectangle"
+    (cartesian_rectangle(axis, axis_value, origin[:2], end[:2], space)), "line"
+    (cartesian_line_inclusive(origin, end, space)) or "cylinder"
+    (cartesian_cylinder(axis, axis_value, origin[:2], radius, height, space))."""
+    kinds = {"volume": PBF_ARRANGE_VOLUME, "rectangle": PBF_ARRANGE_RECTANGLE, "line": PBF_ARRANGE_LINE,
+             "cylinder": PBF_ARRANGE_CYLINDER}
+    a = PbfArrangement()
+    a.kind = kinds[kind]
+    a.axis = _AXES[axis]
+    o = list(origin) + [0.0] * (3 - len(origin))
+    e = list(end) + [0.0] * (3 - len(end))
+    for c in range(3):
+        a.origin[c] = o[c]
+        a.end[c] = e[c]
+    a.axis_value, a.radius, a.height, a.space = axis_value, radius, height, space
+    return a
+
+
+def arrangement_count(a: PbfArrangement) -> int:
+    n = ctypes.c_uint32()
+    check(load().pbf_arrangement_count(ctypes.byref(a), ctypes.byref(n)), "pbf_arrangement_count")
+    return n.value
+
+
+class Emitter:
+    """A fixed set of particles resident on a device, appended by
+    PbfParticle.emit / Batch.emit (the sphere scene's jet,
+    src/simulator/sphere/pbf_sphere_sim.cpp:20-82)."""
+
+    def __init__(self, x=None, v=None, *, arrangement: PbfArrangement | None = None, velocity=(0.0, 0.0, 0.0),
+                 device: int = 0):
+        h = ctypes.c_void_p()
+        if arrangement is not None:
+            check(load().pbf_emitter_create_arrangement(device, ctypes.byref(arrangement), _f3(velocity),
+                                                        ctypes.byref(h)), "pbf_emitter_create_arrangement")
+        else:
+            dev = _is_device(x)
+            if not dev:
+                x, v = _host3(x), _host3(v)
+            check(load().pbf_emitter_create(device, _ptr(x), _ptr(v), x.shape[0], 1 if dev else 0,
+                                            ctypes.byref(h)), "pbf_emitter_create")
+        self.handle = h.value
+        self.device = device
+
+    @property
+    def size(self) -> int:
+        n = ctypes.c_uint32()
+        check(load().pbf_emitter_size(self.handle, ctypes.byref(n)), "pbf_emitter_size")
+        return n.value
+
+    def __del__(self):
+        h, self.handle = getattr(self, "handle", None), None
+        if h:
+            try:
+                load().pbf_emitter_destroy(h)
+            except Exception:
+                pass
+
+
+def _scatter_out(fn, args, n_out: int, stream, what: str):
+    x = np.zeros((n_out, 3), np.float32)
+    v = np.zeros((n_out, 3), np.float32)
+    x[:] = np.nan
+    v[:] = np.nan
+    check(fn(*args, x.ctypes.data, v.ctypes.data, int(n_out), 0, _stream(stream)), what)
+    return x, v
 
 
 class Boundary:
@@ -240,6 +315,37 @@ class PbfParticle:
         check(load().pbf_last_launches(self.handle, ctypes.byref(n)), "pbf_last_launches")
         return n.value
 
+    # -- ids, order restore, device-side appends
+    def particle_ids(self, stream=None) -> np.ndarray:
+        """Id of each particle in its current (sorted) order."""
+        n = self.num
+        ids = np.zeros(n, np.uint32)
+        if n:
+            check(load().pbf_get_particle_ids(self.handle, ids.ctypes.data, 0, _stream(stream)),
+                  "pbf_get_particle_ids")
+        return ids
+
+    def restore_order(self, n_out: int, stream=None):
+        """restoreOrder: positions / velocities in the order of the last
+        step's input (rows without a live particle are NaN)."""
+        return _scatter_out(load().pbf_restore_order, (self.handle,), n_out, stream, "pbf_restore_order")
+
+    def particles_by_id(self, n_out: int, stream=None):
+        """Row k = the particle with id k (NaN where no live particle has it)."""
+        return _scatter_out(load().pbf_get_particles_by_id, (self.handle,), n_out, stream,
+                            "pbf_get_particles_by_id")
+
+    def generate(self, a: PbfArrangement, velocity=(0.0, 0.0, 0.0), stream=None) -> int:
+        """Append an arrangement's points on the device; returns its point count."""
+        n = ctypes.c_uint32()
+        check(load().pbf_generate(self.handle, ctypes.byref(a), _f3(velocity), _stream(stream), ctypes.byref(n)),
+              "pbf_generate")
+        return n.value
+
+    def emit(self, emitter: Emitter, max_fill: float = 0.8, stream=None):
+        """Append the emitter's particles iff num < max_fill * capacity, decided on the device."""
+        check(load().pbf_emit(self.handle, emitter.handle, float(max_fill), _stream(stream)), "pbf_emit")
+
     def neighbor_debug(self) -> dict:
         """Integer intermediates of the last step in the reference's layouts
         (neighbor_search getters, src/pbf/interaction/pbf_neighbor_search.h:49-56)."""
@@ -358,6 +464,34 @@ class Batch:
         check(load().pbf_batch_get_scene(self.handle, sid, _ptr(x_out), _ptr(v_out), ctypes.byref(n), 1,
                                          _stream(stream)), "pbf_batch_get_scene")
         return n.value
+
+    def particle_ids(self, sid: int, stream=None) -> np.ndarray:
+        n = ctypes.c_uint32()
+        check(load().pbf_batch_get_particle_ids(self.handle, sid, None, ctypes.byref(n), 0, _stream(stream)),
+              "pbf_batch_get_particle_ids")
+        ids = np.zeros(n.value, np.uint32)
+        if n.value:
+            check(load().pbf_batch_get_particle_ids(self.handle, sid, ids.ctypes.data, ctypes.byref(n), 0,
+                                                    _stream(stream)), "pbf_batch_get_particle_ids")
+        return ids[:n.value]
+
+    def restore_order(self, sid: int, n_out: int, stream=None):
+        return _scatter_out(load().pbf_batch_restore_order, (self.handle, sid), n_out, stream,
+                            "pbf_batch_restore_order")
+
+    def particles_by_id(self, sid: int, n_out: int, stream=None):
+        return _scatter_out(load().pbf_batch_get_particles_by_id, (self.handle, sid), n_out, stream,
+                            "pbf_batch_get_particles_by_id")
+
+    def generate(self, sid: int, a: PbfArrangement, velocity=(0.0, 0.0, 0.0), stream=None) -> int:
+        n = ctypes.c_uint32()
+        check(load().pbf_batch_generate(self.handle, sid, ctypes.byref(a), _f3(velocity), _stream(stream),
+                                        ctypes.byref(n)), "pbf_batch_generate")
+        return n.value
+
+    def emit(self, sid: int, emitter: Emitter, max_fill: float = 0.8, stream=None):
+        check(load().pbf_batch_emit(self.handle, sid, emitter.handle, float(max_fill), _stream(stream)),
+              "pbf_batch_emit")
 
     def flags(self, sid: int, clear: bool = False) -> int:
         f = ctypes.c_uint32()

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpbf103.so")
 
-SOURCES = ["pbf_kernels.cu", "pbf_engine.cu", "pbf_capi.cu", "pbf_server.cu", "pbf_noalloc.cu"]
+SOURCES = ["pbf_kernels.cu", "pbf_engine.cu", "pbf_capi.cu", "pbf_server.cu", "pbf_noalloc.cu", "pbf_particles.cu"]
 HEADERS = ["pbf_internal.h", "pbf_engine.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -163,8 +163,8 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
 
 uint64_t bytes_per_particle(uint32_t max_pair)
 {
-    // x v xs xa xb xold w vt (float4) + key slot tmp perm + lam + nnb + nbr
-    return 8 * 16 + 4 * 4 + 4 + 1 + 4ull * (max_pair - 1);
+    // x v xs xa xb xold w vt (float4) + key slot tmp perm id id_tmp + lam + nnb + nbr
+    return 8 * 16 + 6 * 4 + 4 + 1 + 4ull * (max_pair - 1);
 }
 
 // ---------------------------------------------------------------- batch --
@@ -176,7 +176,8 @@ Batch::~Batch()
     if (h_small_) cudaFreeHost(h_small_);
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
-                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_};
+                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
+                    d_next_id_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -210,9 +211,10 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_ctrl_, sizeof(Ctrl)));
     CK(A((void **)&d_scene_num_, 4ull * max_scenes));
     CK(A((void **)&d_flags_, 4ull * max_scenes));
+    CK(A((void **)&d_next_id_, 4ull * max_scenes));
     float4 **f4[] = {&d_x_, &d_v_, &d_xs_, &d_xa_, &d_xb_, &d_xold_, &d_w_, &d_vt_};
     for (float4 **p : f4) CK(A((void **)p, 16 * P));
-    uint32_t **u4[] = {&d_key_, &d_slot_, &d_tmp_, &d_perm_};
+    uint32_t **u4[] = {&d_key_, &d_slot_, &d_tmp_, &d_perm_, &d_id_, &d_id_tmp_};
     for (uint32_t **p : u4) CK(A((void **)p, 4 * P));
     CK(A((void **)&d_count_, 4 * (C + 4)));
     CK(A((void **)&d_offsets_, 4 * (C + 4)));
@@ -228,6 +230,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(cudaMemset(d_offsets_, 0, 4 * (C + 4)));
     CK(cudaMemset(d_scene_num_, 0, 4ull * max_scenes));
     CK(cudaMemset(d_flags_, 0, 4ull * max_scenes));
+    CK(cudaMemset(d_next_id_, 0, 4ull * max_scenes));
     CK(cudaMemset(d_ctrl_, 0, sizeof(Ctrl)));
     CK(cudaMemset(d_nnb_, 0, P));
     CK(cudaMemset(d_v_, 0, 16 * P));
@@ -385,6 +388,11 @@ pbf_status Batch::set_particles(uint32_t id, const float *x, const float *v, uin
         else CK(cudaMemsetAsync(dv, 0, 16ull * n, st));
         CK(cudaGetLastError());
     }
+    // ids: a fresh set numbers the particles 0..n-1; an append continues
+    // from the scene's device-side counter
+    launch_assign_ids(d_id_ + s.desc.p_off + start, d_next_id_ + id, n, append, st);
+    CK(cudaGetLastError());
+    s.perm_valid = false;
     const uint32_t total = start + n;
     launch_set_u32(d_scene_num_ + id, total, st);
     CK(cudaGetLastError());
@@ -425,6 +433,7 @@ pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float
         tot += c;
         if (s.num_upper != c) dirty_tiles_ = true;
         s.num_upper = c;
+        s.perm_valid = false;
     }
     CK(cudaMemcpyAsync(d_pack_off_, pack, 4 * ns, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_scene_num_, nums, 4 * ns, cudaMemcpyHostToDevice, st));
@@ -441,6 +450,10 @@ pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float
         }
     }
     if (ctrl_.n_tiles) launch_unpack(args(), shape_for(tile_), d_pack_off_, sx, sv, st);
+    CK(cudaGetLastError());
+    // k_unpack restarts the id counters of scenes with particles; the rest here
+    for (size_t k = 0; k < ids.size(); ++k)
+        if (scenes_[ids[k]].num_upper == 0) launch_set_u32(d_next_id_ + ids[k], 0, st);
     CK(cudaGetLastError());
     return PBF_SUCCESS;
 }
@@ -646,6 +659,9 @@ StepArgs Batch::args() const
     a.xa = d_xa_;
     a.xb = d_xb_;
     a.xold = d_xold_;
+    a.id = d_id_;
+    a.id_tmp = d_id_tmp_;
+    a.next_id = d_next_id_;
     a.lam = d_lam_;
     a.nbr = d_nbr_;
     a.nnb = d_nnb_;
@@ -774,7 +790,39 @@ pbf_status Batch::step(int iters, cudaStream_t st)
         last_launches_ = 0;
         return PBF_SUCCESS;
     }
-    return run(iters, st, true);
+    rc = run(iters, st, true);
+    if (rc == PBF_SUCCESS)
+        for (auto &s : scenes_) s.perm_valid = s.active;
+    return rc;
+}
+
+pbf_status Batch::scene_arrays(uint32_t id, SceneArrays *o)
+{
+    if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
+    const SceneDesc &d = scenes_[id].desc;
+    o->x = d_x_ + d.p_off;
+    o->v = d_v_ + d.p_off;
+    o->id = d_id_ + d.p_off;
+    o->perm = d_perm_ + d.p_off;
+    o->stage = d_xs_ + d.p_off;
+    o->scene_num = d_scene_num_ + id;
+    o->next_id = d_next_id_ + id;
+    o->flags = d_flags_ + id;
+    o->offsets = d_offsets_ + d.c_off;
+    o->p_off = d.p_off;
+    o->capacity = d.capacity;
+    o->c_off = d.c_off;
+    o->ncell = d.ncell;
+    return PBF_SUCCESS;
+}
+
+void Batch::note_append(uint32_t id, uint32_t n)
+{
+    SceneHost &s = scenes_[id];
+    const uint32_t up = (uint32_t)std::min<uint64_t>((uint64_t)s.num_upper + n, s.desc.capacity);
+    if (up != s.num_upper) dirty_tiles_ = true;
+    s.num_upper = up;
+    s.perm_valid = false;
 }
 
 pbf_status Batch::get_num(uint32_t id, uint32_t *num, cudaStream_t st)

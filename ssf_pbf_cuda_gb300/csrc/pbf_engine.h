@@ -43,6 +43,7 @@ struct SceneHost {
     uint64_t cells = 0;       // ncell + 1 (deleted bucket)
     uint64_t bnd_len = 0;     // float4s in the boundary pool
     uint64_t bnd_off = 0;
+    bool perm_valid = false;  // perm holds the last step's permutation of this scene's input
 };
 
 pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc *d, uint32_t grid[3]);
@@ -78,6 +79,17 @@ public:
     pbf_status upload_all(const uint32_t *counts, const float *x, const float *v, bool src_dev, cudaStream_t st);
     pbf_status download_all(uint32_t *counts, float *x, float *v, bool dst_dev, cudaStream_t st);
     pbf_status import_x_device(uint32_t id, const float *x_dev, uint32_t n, cudaStream_t st);
+    // device arrays of one scene, for the particle-set operations (pbf_particles.cu)
+    struct SceneArrays {
+        float4 *x, *v;
+        uint32_t *id, *perm, *scene_num, *next_id, *flags, *offsets;
+        float4 *stage;         // the scene's xs slice: free between steps
+        uint32_t p_off, capacity, c_off, ncell;
+    };
+    pbf_status scene_arrays(uint32_t id, SceneArrays *out);
+    // host bookkeeping after a device-side append of up to n particles
+    void note_append(uint32_t id, uint32_t n);
+    bool perm_valid(uint32_t id) const { return id < scenes_.size() && scenes_[id].perm_valid; }
     pbf_status export_x_device(uint32_t id, float *x_dev, cudaStream_t st);
     pbf_status autotune(int iters, cudaStream_t st, uint32_t *chosen);
     // one step without a graph, with events between kernels
@@ -123,6 +135,8 @@ private:
     uint8_t *d_nnb_ = nullptr;
     float4 *d_bnd_ = nullptr;
     uint32_t *d_pack_off_ = nullptr;  // per-scene packed offsets for set_all/get_all
+    uint32_t *d_id_ = nullptr, *d_id_tmp_ = nullptr;  // particle ids, phase order / sorted scratch
+    uint32_t *d_next_id_ = nullptr;                   // per scene: next id to hand out
     uint32_t *h_small_ = nullptr;     // pinned host scratch: pack offsets + counts
     cudaEvent_t small_done_ = nullptr;
     uint64_t bnd_capacity_ = 0;

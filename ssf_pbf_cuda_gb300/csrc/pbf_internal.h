@@ -79,6 +79,8 @@ struct StepArgs {
     uint8_t *nnb;
     float4 *w, *vt;               // vorticity, XSPH velocity scratch
     const float4 *bnd;            // boundary primitives
+    uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
+    uint32_t *next_id;            // per scene: id of the next particle added
     uint64_t nbr_stride;
 };
 
@@ -126,6 +128,8 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, uint32
 void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st);
 void launch_f4_to_aos3(const float4 *src, float *dst, uint32_t n, cudaStream_t st);
 void launch_set_u32(uint32_t *dst, uint32_t value, cudaStream_t st);
+// ids of n particles added at dst: append ? *next_id + k : k; *next_id += / = n.
+void launch_assign_ids(uint32_t *dst, uint32_t *next_id, uint32_t n, bool append, cudaStream_t st);
 // Whole-batch moves between a packed AoS float3 buffer (active scenes in
 // slot order, pack_off[s] = first packed particle of scene s) and the
 // scene-sliced float4 phase arrays.  unpack uses the tile list (counts must

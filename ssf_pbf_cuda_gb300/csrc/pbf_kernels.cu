@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     a.perm[g] = local;
     a.xa[g] = a.xs[i];
     a.xold[g] = a.x[i];
+    a.id_tmp[g] = a.id[i];
     TILE_LOOP_END
 }
 
@@ -656,6 +657,7 @@ __global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restr
     if (last) {
         const float4 xo_ = a.xold[i];
         vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+        a.id[i] = a.id_tmp[i];  // ids follow the particles into sorted order
     }
     TILE_LOOP_END
 }
@@ -674,6 +676,7 @@ __global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict
     const float4 xo_ = a.xold[i];
     a.x[i] = xn;
     vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+    a.id[i] = a.id_tmp[i];
     TILE_LOOP_END
 }
 
@@ -875,6 +878,8 @@ __global__ void __launch_bounds__(512) k_unpack(StepArgs a, const uint32_t *__re
     const uint32_t i = a.scenes[s].p_off + local;
     a.x[i] = make_float4(sx[3 * q], sx[3 * q + 1], sx[3 * q + 2], 0.f);
     a.v[i] = sv ? make_float4(sv[3 * q], sv[3 * q + 1], sv[3 * q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    a.id[i] = local;  // a whole-scene upload numbers the particles afresh
+    if (local == 0) a.next_id[s] = n;
     TILE_LOOP_END
 }
 
