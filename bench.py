@@ -265,7 +265,19 @@ def run_ns_microbench(api, device: int, reps: int = 3) -> dict:
     return out
 
 
+def workload_config(n_scenes: int, particles: int, cells: int, world: int) -> dict:
+    """The batched workload as both arms name it."""
+    return {"workload": f"batched: {n_scenes} dam-break scenes per GPU, 4k-64k particles "
+                        f"(log-uniform, seeded), {ITERS} iterations, s_corr k=0.1 n=4 dq=0.2h, "
+                        "XSPH 0.01, vorticity 0.0005, eps 600, dt 1/120",
+            "particles_per_gpu": particles, "cells_per_gpu": cells,
+            "l2": "inputs larger than L2 (per-step working set >> 129 MB)",
+            "step_definition": "seeded initial state re-loaded, then one full step",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
+    import numpy as np
     rank, world, _ = env_rank()
     if rank != 0:
         return
@@ -298,8 +310,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded dam-break scenes)",
-        "config": {"workload": "batched: 256 dam-break scenes, 4k-64k particles (log-uniform), 4 iterations",
-                   "sample_particles": tot, "sample_scenes": len(sample)},
+        "config": dict(workload_config(len(scs), sum(sc.n for sc in scs),
+                                       sum(int(np.prod(scene_params(sc)["grid_size"])) + 1 for sc in scs), 1),
+                       sample_particles=tot, sample_scenes=len(sample)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"first {len(sample)} scenes ({tot} particles) of the batched workload, "
                                    f"one step each per timed step"},
@@ -549,13 +562,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break scenes, no dataset)",
-            "config": {"workload": f"batched: {len(scs)} dam-break scenes per GPU, 4k-64k particles "
-                                   f"(log-uniform, seeded), {ITERS} iterations, s_corr k=0.1 n=4 dq=0.2h, "
-                                   "XSPH 0.01, vorticity 0.0005, eps 600, dt 1/120",
-                       "particles_per_gpu": n_total, "cells_per_gpu": cells, "tile": tile, "chunk": shape["chunk"],
-                       "l2": "inputs larger than L2 (per-step working set >> 129 MB)",
-                       "step_definition": "device-resident initial state re-loaded, then one full step",
-                       "parallelism": f"replicas x{world}"},
+            "config": dict(workload_config(len(scs), n_total, cells, world),
+                           tile=tile, chunk=shape["chunk"]),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
             "serving": serving, "ns_microbench": ns_micro,
             "gpu_launches": launches_per_step * args.steps,
