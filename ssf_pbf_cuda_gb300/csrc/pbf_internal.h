@@ -80,6 +80,9 @@ struct StepArgs {
     float4 *w, *vt;               // vorticity, XSPH velocity scratch
     const float4 *bnd;            // boundary primitives
     uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
+    uint8_t *cls, *tcls;          // alias class of each particle (input order / bucket slot order)
+    float4 *wx;                   // walk copy: sorted positions grouped by alias class per bucket, .w = slot
+    uint64_t *chist;              // per cell: 8 x 8-bit class counts of its bucket, or kClassWhole
     uint32_t *next_id;            // per scene: id of the next particle added
     uint64_t nbr_stride;
 };
@@ -138,6 +141,10 @@ void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pac
                    const float *src_v, cudaStream_t st);
 void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, float *dst_x, float *dst_v,
                  cudaStream_t st);
+
+// chist value of a bucket whose walk copy is in plain sorted order (more
+// than 255 members, or a bucket left in atomic order)
+constexpr uint64_t kClassWhole = ~0ull;
 
 constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;

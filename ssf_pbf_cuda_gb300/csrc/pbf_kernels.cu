@@ -39,6 +39,18 @@ __device__ __forceinline__ uint32_t hash3(uint32_t x, uint32_t y, uint32_t z, co
     return z * d.gx * d.gy + y * d.gx + x;
 }
 
+// Alias class of a cell: which of the 2 x 2 x 2 periodic copies of the
+// power-of-two table the (unwrapped) cell lies in.  With the table sized for
+// cells of 2h (calcGridSize, pbf_type.cpp:141-162) but cells h wide, a
+// bucket holds particles of cells G apart; only one class of a bucket can
+// hold neighbours of a given cell.  Cells 2G apart share a class; they are
+// far apart, so the distance test still rejects them.
+__device__ __forceinline__ uint32_t alias_class(int32_t cx, int32_t cy, int32_t cz, const SceneDesc &d)
+{
+    const int sx = __ffs(d.gx) - 1, sy = __ffs(d.gy) - 1, sz = __ffs(d.gz) - 1;
+    return (uint32_t)(((cz >> sz) & 1) << 2 | ((cy >> sy) & 1) << 1 | ((cx >> sx) & 1));
+}
+
 // r^2 exactly as findPair computes it (pbf_neighbor_search_util.cu:398):
 // fmaf(dz, dz, fmaf(dy, dy, dx * dx)), no further contraction.
 __device__ __forceinline__ float dist2_exact(float4 a, float4 b)
@@ -237,6 +249,70 @@ __device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t
     }
 }
 
+// The neighbour-search walk over the class-grouped walk copy (wx): the same
+// 27 cells in the same order as walk27_ranges, one range per cell, and inside
+// a cell's bucket only the sub-range of the cell's alias class (chist holds
+// the bucket's class counts).  Candidates of the other classes lie at least
+// G - 1 cells away and can never be accepted, and the walk copy keeps each
+// class in sorted order, so the accepted sequence is the reference's.
+// Buckets marked kClassWhole (and every bucket of a scene with an axis of
+// fewer than 4 cells, where the reference visits wrapped cells twice) are
+// visited whole, in sorted order.  PRUNE as in walk27_ranges.
+template <bool PRUNE, class R>
+__device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t *__restrict__ offsets,
+                                             const uint64_t *__restrict__ chist, uint32_t shift, float4 xp, R &&r)
+{
+    const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
+    const bool prune = PRUNE && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+    float lx = 0.f, ly = 0.f, lz = 0.f, rx = 0.f, ry = 0.f, rz = 0.f;
+    if (prune) {
+        lx = xp.x - (float)icx * d.cw;
+        ly = xp.y - (float)icy * d.cw;
+        lz = xp.z - (float)icz * d.cw;
+        rx = d.cw - lx;
+        ry = d.cw - ly;
+        rz = d.cw - lz;
+    }
+    const float lim = d.h2 * 1.001f;
+    const int sx = __ffs(d.gx) - 1, sy = __ffs(d.gy) - 1, sz = __ffs(d.gz) - 1;
+    const uint32_t *off = offsets + d.c_off;
+    const uint64_t *ch = chist + d.c_off;
+#pragma unroll 1
+    for (int rr = 0; rr < 9; ++rr) {
+        const int dz = rr / 3 - 1, dy = rr % 3 - 1;
+        bool left = true, right = true;
+        if (prune) {
+            const float ez = dz < 0 ? lz : (dz > 0 ? rz : 0.f);
+            const float ey = dy < 0 ? ly : (dy > 0 ? ry : 0.f);
+            const float eyz2 = ey * ey + ez * ez;
+            if (eyz2 > lim) continue;
+            left = eyz2 + lx * lx <= lim;
+            right = eyz2 + rx * rx <= lim;
+        }
+        const int32_t ty = icy + dy, tz = icz + dz;
+        const uint32_t row = ((uint32_t)tz & (d.gz - 1u)) * d.gx * d.gy + ((uint32_t)ty & (d.gy - 1u)) * d.gx;
+        const uint32_t cyz = (uint32_t)(((tz >> sz) & 1) << 2 | ((ty >> sy) & 1) << 1);
+#pragma unroll 1
+        for (int dx = -1; dx <= 1; ++dx) {
+            if ((dx < 0 && !left) || (dx > 0 && !right)) continue;
+            const int32_t tx = icx + dx;
+            const uint32_t b = row + ((uint32_t)tx & (d.gx - 1u));
+            uint32_t st = __ldg(off + b);
+            uint32_t en = __ldg(off + b + 1);
+            if (st == en) continue;
+            const uint64_t h = __ldg(reinterpret_cast<const unsigned long long *>(ch + b));
+            if (h != kClassWhole) {
+                const uint32_t sh = 8u * (cyz | (uint32_t)((tx >> sx) & 1));
+                const uint64_t lower = sh ? (h & ((1ull << sh) - 1ull)) : 0ull;
+                st += (uint32_t)((lower * 0x0101010101010101ull) >> 56);  // byte sum: bucket <= 255
+                en = st + (uint32_t)((h >> sh) & 0xFFull);
+                if (st == en) continue;
+            }
+            if (!r(st + shift, en + shift)) return;
+        }
+    }
+}
+
 // walk27 with the per-neighbour work taken out of the walk: candidates that
 // pass accept(j) are queued in a small per-thread buffer and handed to use(j)
 // in batches, so the neighbour math is not executed masked for every
@@ -321,11 +397,15 @@ __global__ void __launch_bounds__(512) k_predict_hash(StepArgs a)
     ps.y = __fmaf_rn(__fmaf_rn(d.g[1], dt, vv.y), dt, xv.y);
     ps.z = __fmaf_rn(__fmaf_rn(d.g[2], dt, vv.z), dt, xv.z);
     ps.w = 0.f;
-    uint32_t key = hash3((uint32_t)cell_coord(ps.x, d.cw), (uint32_t)cell_coord(ps.y, d.cw),
-                         (uint32_t)cell_coord(ps.z, d.cw), d);
+    const int32_t cx = cell_coord(ps.x, d.cw), cy = cell_coord(ps.y, d.cw), cz = cell_coord(ps.z, d.cw);
+    uint32_t key = hash3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz, d);
+    uint32_t cls = alias_class(cx, cy, cz, d);
     if (ps.x < d.amin[0] || d.amax[0] < ps.x || ps.y < d.amin[1] || d.amax[1] < ps.y || ps.z < d.amin[2] ||
-        d.amax[2] < ps.z)
+        d.amax[2] < ps.z) {
         key = d.ncell;
+        cls = 0;
+    }
+    a.cls[i] = (uint8_t)cls;
     if (!(isfinite(ps.x) && isfinite(ps.y) && isfinite(ps.z))) atomicOr(a.flags + s, PBF_FLAG_NONFINITE);
     a.xs[i] = ps;
     a.key[i] = key;
@@ -447,7 +527,9 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
     if (local >= n) continue;
     const SceneDesc d = a.scenes[s];
     const uint32_t i = d.p_off + local;
-    a.tmp[a.offsets[d.c_off + a.key[i]] + a.slot[i]] = local;
+    const uint32_t pos = a.offsets[d.c_off + a.key[i]] + a.slot[i];
+    a.tmp[pos] = local;
+    a.tcls[pos] = a.cls[i];
     TILE_LOOP_END
 }
 
@@ -468,17 +550,36 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     const uint32_t i = d.p_off + local;
     const uint32_t gk = d.c_off + a.key[i];
     const uint32_t st = a.offsets[gk], en = a.offsets[gk + 1];
-    uint32_t rank;
+    // rank: members with a smaller input index (stable sorted order); for the
+    // walk copy also members of a smaller class, members of the same class
+    // with a smaller input index, and the bucket's class histogram
+    const uint32_t my_cls = a.cls[i];
+    uint32_t rank, below = 0, frank = 0;
+    uint64_t hist = 0;
+    const bool grouped = en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
     if (en - st <= kStableLimit) {
         rank = 0;
-        for (uint32_t t = st; t < en; ++t) rank += (__ldg(a.tmp + t) < local) ? 1u : 0u;
+        for (uint32_t t = st; t < en; ++t) {
+            const uint32_t m = __ldg(a.tmp + t);
+            const uint32_t mc = __ldg(a.tcls + t);
+            const bool smaller = m < local;
+            rank += smaller ? 1u : 0u;
+            below += (mc < my_cls) ? 1u : 0u;
+            frank += (mc == my_cls && smaller) ? 1u : 0u;
+            hist += 1ull << (8u * mc);
+        }
     } else {
         rank = a.slot[i];
     }
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t g = d.p_off + (st - base) + rank;
+    const float4 ps = a.xs[i];
+    // walk copy: grouped by class inside the bucket, or in sorted order
+    const uint32_t w = grouped ? d.p_off + (st - base) + below + frank : g;
+    a.wx[w] = make_float4(ps.x, ps.y, ps.z, __uint_as_float(g));
+    if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
     a.perm[g] = local;
-    a.xa[g] = a.xs[i];
+    a.xa[g] = ps;
     a.xold[g] = a.x[i];
     a.id_tmp[g] = a.id[i];
     TILE_LOOP_END
@@ -504,24 +605,26 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     const uint64_t stride = a.nbr_stride;
     uint32_t *nl = a.nbr + i;
     const float4 *__restrict__ xa = a.xa;
+    const float4 *__restrict__ wx = a.wx;
     // phase 1: the walk only tests and records (lanes of a warp accept
     // different candidates, so pair math inside the walk would run masked
-    // for almost every candidate)
+    // for almost every candidate); candidates come from the walk copy, whose
+    // .w is the candidate's sorted index
     // Candidates are fetched kNbFetch at a time (more loads in flight) and
     // tested in order, so the first `cap` accepted ones are the reference's.
     constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
     uint32_t *slot = nl;
-    walk27_ranges<true>(d, a.offsets, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
+    walk27_cells<true>(d, a.offsets, a.chist, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
             float4 c[kNbFetch];
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k)
-                if (q0 + k < en) c[k] = __ldg(xa + q0 + k);
+                if (q0 + k < en) c[k] = __ldg(wx + q0 + k);
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
-                    *slot = q0 + k;
+                    *slot = __float_as_uint(c[k].w);
                     slot += stride;
                     if (++cnt == cap) return false;
                 }
