@@ -137,7 +137,7 @@ private:
     uint32_t *d_pack_off_ = nullptr;  // per-scene packed offsets for set_all/get_all
     uint32_t *d_id_ = nullptr, *d_id_tmp_ = nullptr;  // particle ids, phase order / sorted scratch
     uint32_t *d_next_id_ = nullptr;                   // per scene: next id to hand out
-    uint8_t *d_cls_ = nullptr, *d_tcls_ = nullptr;    // alias classes (input order / bucket slots)
+    uint8_t *d_cls_ = nullptr;                        // alias class per particle (input order)
     float4 *d_wx_ = nullptr;                          // class-grouped walk copy of the sorted positions
     uint64_t *d_chist_ = nullptr;                     // per cell: class counts of its bucket
     uint32_t *h_small_ = nullptr;     // pinned host scratch: pack offsets + counts

@@ -80,8 +80,8 @@ struct StepArgs {
     float4 *w, *vt;               // vorticity, XSPH velocity scratch
     const float4 *bnd;            // boundary primitives
     uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
-    uint8_t *cls, *tcls;          // alias class of each particle (input order / bucket slot order)
-    float4 *wx;                   // walk copy: sorted positions grouped by alias class per bucket, .w = slot
+    uint8_t *cls;                 // alias class of each particle (input order)
+    float4 *wx;                   // walk copy of mixed-class buckets: grouped by class, .w = sorted slot
     uint64_t *chist;              // per cell: 8 x 8-bit class counts of its bucket, or kClassWhole
     uint32_t *next_id;            // per scene: id of the next particle added
     uint64_t nbr_stride;

@@ -249,18 +249,22 @@ __device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t
     }
 }
 
-// The neighbour-search walk over the class-grouped walk copy (wx): the same
-// 27 cells in the same order as walk27_ranges, one range per cell, and inside
-// a cell's bucket only the sub-range of the cell's alias class (chist holds
-// the bucket's class counts).  Candidates of the other classes lie at least
-// G - 1 cells away and can never be accepted, and the walk copy keeps each
-// class in sorted order, so the accepted sequence is the reference's.
-// Buckets marked kClassWhole (and every bucket of a scene with an axis of
-// fewer than 4 cells, where the reference visits wrapped cells twice) are
-// visited whole, in sorted order.  PRUNE as in walk27_ranges.
+// The neighbour-search walk: the same 27 cells in the same order as
+// walk27_ranges, one range per cell, and inside a cell's bucket only the
+// particles of the cell's alias class (chist holds the bucket's class
+// counts): a bucket of one class is the sorted range itself (xa), a bucket
+// without the class is skipped, and a mixed bucket gives the class's
+// sub-range of the class-grouped walk copy (wx).  Candidates of the other
+// classes lie at least G - 1 cells away and can never be accepted, and both
+// arrays keep each class in sorted order with the sorted slot in .w, so the
+// accepted sequence is the reference's.  Buckets marked kClassWhole (and
+// every bucket of a scene with an axis of fewer than 4 cells, where the
+// reference visits wrapped cells twice) are visited whole, in sorted order.
+// r(src, st, en) gets the array and the range.  PRUNE as in walk27_ranges.
 template <bool PRUNE, class R>
 __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t *__restrict__ offsets,
-                                             const uint64_t *__restrict__ chist, uint32_t shift, float4 xp, R &&r)
+                                             const uint64_t *__restrict__ chist, const float4 *xa,
+                                             const float4 *wx, uint32_t shift, float4 xp, R &&r)
 {
     const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
     const bool prune = PRUNE && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
@@ -301,14 +305,19 @@ __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t 
             uint32_t en = __ldg(off + b + 1);
             if (st == en) continue;
             const uint64_t h = __ldg(reinterpret_cast<const unsigned long long *>(ch + b));
+            const float4 *src = xa;
             if (h != kClassWhole) {
                 const uint32_t sh = 8u * (cyz | (uint32_t)((tx >> sx) & 1));
-                const uint64_t lower = sh ? (h & ((1ull << sh) - 1ull)) : 0ull;
-                st += (uint32_t)((lower * 0x0101010101010101ull) >> 56);  // byte sum: bucket <= 255
-                en = st + (uint32_t)((h >> sh) & 0xFFull);
-                if (st == en) continue;
+                const uint32_t cnt = (uint32_t)((h >> sh) & 0xFFull);
+                if (cnt == 0) continue;  // no particle of this cell in the bucket
+                if (cnt != en - st) {    // several classes: this one's sub-range of the walk copy
+                    const uint64_t lower = sh ? (h & ((1ull << sh) - 1ull)) : 0ull;
+                    st += (uint32_t)((lower * 0x0101010101010101ull) >> 56);  // byte sum: bucket <= 255
+                    en = st + cnt;
+                    src = wx;
+                }
             }
-            if (!r(st + shift, en + shift)) return;
+            if (!r(src, st + shift, en + shift)) return;
         }
     }
 }
@@ -518,6 +527,11 @@ __global__ void __launch_bounds__(256) k_scan_down(StepArgs a)
     }
 }
 
+// tmp entries of scenes up to kClsLimit particles carry the member's alias
+// class above its input index.
+constexpr uint32_t kClsShift = 29;
+constexpr uint32_t kClsLimit = 1u << kClsShift;
+
 // Scatter into the cell buckets in atomic-slot order (sortByCountingCUDA,
 // pbf_counting_sort.cu:120-134).
 __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
@@ -528,8 +542,8 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
     const SceneDesc d = a.scenes[s];
     const uint32_t i = d.p_off + local;
     const uint32_t pos = a.offsets[d.c_off + a.key[i]] + a.slot[i];
-    a.tmp[pos] = local;
-    a.tcls[pos] = a.cls[i];
+    // the alias class rides in the top bits (scenes below 2^29 particles)
+    a.tmp[pos] = d.capacity <= kClsLimit ? local | ((uint32_t)a.cls[i] << kClsShift) : local;
     TILE_LOOP_END
 }
 
@@ -553,20 +567,22 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     // rank: members with a smaller input index (stable sorted order); for the
     // walk copy also members of a smaller class, members of the same class
     // with a smaller input index, and the bucket's class histogram
+    const bool packed = d.capacity <= kClsLimit;
+    const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
     const uint32_t my_cls = a.cls[i];
     uint32_t rank, below = 0, frank = 0;
     uint64_t hist = 0;
-    const bool grouped = en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+    const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
     if (en - st <= kStableLimit) {
         rank = 0;
         for (uint32_t t = st; t < en; ++t) {
-            const uint32_t m = __ldg(a.tmp + t);
-            const uint32_t mc = __ldg(a.tcls + t);
+            const uint32_t e = __ldg(a.tmp + t);
+            const uint32_t m = e & imask, mc = e >> kClsShift;
             const bool smaller = m < local;
             rank += smaller ? 1u : 0u;
             below += (mc < my_cls) ? 1u : 0u;
             frank += (mc == my_cls && smaller) ? 1u : 0u;
-            hist += 1ull << (8u * mc);
+            hist += 1ull << (8u * (mc & 7u));
         }
     } else {
         rank = a.slot[i];
@@ -574,12 +590,15 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t g = d.p_off + (st - base) + rank;
     const float4 ps = a.xs[i];
-    // walk copy: grouped by class inside the bucket, or in sorted order
-    const uint32_t w = grouped ? d.p_off + (st - base) + below + frank : g;
-    a.wx[w] = make_float4(ps.x, ps.y, ps.z, __uint_as_float(g));
+    // sorted positions carry their own slot in .w (the neighbour walk records
+    // .w); buckets holding more than one alias class also get the
+    // class-grouped walk copy
+    const float gw = __uint_as_float(g);
+    if (grouped && ((hist >> (8u * my_cls)) & 0xFFull) != en - st)
+        a.wx[d.p_off + (st - base) + below + frank] = make_float4(ps.x, ps.y, ps.z, gw);
     if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
     a.perm[g] = local;
-    a.xa[g] = ps;
+    a.xa[g] = make_float4(ps.x, ps.y, ps.z, gw);
     a.xold[g] = a.x[i];
     a.id_tmp[g] = a.id[i];
     TILE_LOOP_END
@@ -608,19 +627,19 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     const float4 *__restrict__ wx = a.wx;
     // phase 1: the walk only tests and records (lanes of a warp accept
     // different candidates, so pair math inside the walk would run masked
-    // for almost every candidate); candidates come from the walk copy, whose
-    // .w is the candidate's sorted index
+    // for almost every candidate); a candidate's .w is its sorted slot
     // Candidates are fetched kNbFetch at a time (more loads in flight) and
     // tested in order, so the first `cap` accepted ones are the reference's.
     constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
     uint32_t *slot = nl;
-    walk27_cells<true>(d, a.offsets, a.chist, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
+    walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
+                       [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
             float4 c[kNbFetch];
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k)
-                if (q0 + k < en) c[k] = __ldg(wx + q0 + k);
+                if (q0 + k < en) c[k] = __ldg(src + q0 + k);
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
