@@ -157,10 +157,15 @@ __device__ __forceinline__ void plane(bool &hit, float3 &dp, float3 o, float3 p,
 // fixed-sphere variant, pbf_constraint.cu:262-315).  old_x is the current
 // position, as in the reference (pbf_response_collision.cu:31).  The
 // reference repeats until no primitive reports a hit; here at most max_coll
-// passes.  Returns false when the bound was reached.
+// passes.  Returns false when the bound was reached.  A pass is a function
+// of dp alone, so a pass that hits but leaves dp bit-for-bit unchanged (a
+// projection too small to move the position, which the reference would
+// repeat forever) would repeat identically up to the bound: the loop stops
+// there with the same dp and the same result.
 __device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, float3 x, float3 &dp)
 {
     for (uint32_t pass = 0; pass < d.max_coll; ++pass) {
+        const float3 before = dp;
         float3 p = make_float3(x.x + dp.x, x.y + dp.y, x.z + dp.z);
         bool hit = false;
         if (d.builtin_sphere) {
@@ -179,6 +184,9 @@ __device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, floa
             }
         }
         if (!hit) return true;
+        if (__float_as_uint(dp.x) == __float_as_uint(before.x) && __float_as_uint(dp.y) == __float_as_uint(before.y) &&
+            __float_as_uint(dp.z) == __float_as_uint(before.z))
+            return false;  // fixed point: every later pass repeats this one
     }
     return false;
 }
