@@ -536,9 +536,11 @@ __global__ void __launch_bounds__(256) k_scan_down(StepArgs a)
 }
 
 // tmp entries of scenes up to kClsLimit particles carry the member's alias
-// class above its input index.
+// class above its input index.  wpos of a particle outside a mixed-class
+// bucket is kNoWalkCopy.
 constexpr uint32_t kClsShift = 29;
 constexpr uint32_t kClsLimit = 1u << kClsShift;
+constexpr uint32_t kNoWalkCopy = 0xFFFFFFFFu;
 
 // Scatter into the cell buckets in atomic-slot order (sortByCountingCUDA,
 // pbf_counting_sort.cu:120-134).
@@ -597,18 +599,36 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     }
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t g = d.p_off + (st - base) + rank;
-    const float4 ps = a.xs[i];
-    // sorted positions carry their own slot in .w (the neighbour walk records
-    // .w); buckets holding more than one alias class also get the
-    // class-grouped walk copy
-    const float gw = __uint_as_float(g);
-    if (grouped && ((hist >> (8u * my_cls)) & 0xFFull) != en - st)
-        a.wx[d.p_off + (st - base) + below + frank] = make_float4(ps.x, ps.y, ps.z, gw);
+    // only 4-byte entries are scattered here; k_gather moves the 16-byte
+    // particle data in sorted order (coalesced writes, as the reference's
+    // reorderDataCUDA gathers).  Buckets holding more than one alias class
+    // also place the particle in the class-grouped walk copy.
+    const bool mixed = grouped && ((hist >> (8u * my_cls)) & 0xFFull) != en - st;
+    a.wpos[g] = mixed ? d.p_off + (st - base) + below + frank : kNoWalkCopy;
     if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
     a.perm[g] = local;
-    a.xa[g] = make_float4(ps.x, ps.y, ps.z, gw);
+    TILE_LOOP_END
+}
+
+// Reorder in sorted order (reorderDataCUDA x2, pbf_neighbor_search_util.cu:143-154):
+// sorted predicted positions (carrying their own slot in .w, which the
+// neighbour walk records), sorted old positions and ids; the walk copy of
+// mixed-class buckets.
+__global__ void __launch_bounds__(512) k_gather(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const SceneDesc d = a.scenes[s];
+    const uint32_t g = d.p_off + local;
+    const uint32_t i = d.p_off + a.perm[g];
+    const float4 ps = a.xs[i];
+    const float4 xg = make_float4(ps.x, ps.y, ps.z, __uint_as_float(g));
+    a.xa[g] = xg;
     a.xold[g] = a.x[i];
     a.id_tmp[g] = a.id[i];
+    const uint32_t w = a.wpos[g];
+    if (w != kNoWalkCopy) a.wx[w] = xg;
     TILE_LOOP_END
 }
 
@@ -1089,7 +1109,7 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
     Occupancy o;
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
-                 mn(occ((const void *)k_rank_reorder), occ((const void *)k_finalize)));
+                 mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
     o.nb = occ((const void *)k_neighbors_lambda);
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
@@ -1146,6 +1166,8 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     PBF_LAUNCHED("k_scatter");
     k_rank_reorder<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_rank_reorder");
+    k_gather<<<g, b, 0, st>>>(a);
+    PBF_LAUNCHED("k_gather");
     k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
     PBF_LAUNCHED("k_neighbors_lambda");
     const bool xsph = (post & (kPostXsphWalk | kPostXsphList)) != 0;
