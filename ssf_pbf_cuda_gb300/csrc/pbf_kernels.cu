@@ -581,18 +581,27 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
     const uint32_t my_cls = a.cls[i];
     uint32_t rank, below = 0, frank = 0;
-    uint64_t hist = 0;
     const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+    uint64_t hist = (uint64_t)(en - st) << (8u * my_cls);  // every member of my class
+    bool mixed = false;
     if (en - st <= kStableLimit) {
         rank = 0;
+        uint32_t diff = 0;
         for (uint32_t t = st; t < en; ++t) {
             const uint32_t e = __ldg(a.tmp + t);
-            const uint32_t m = e & imask, mc = e >> kClsShift;
-            const bool smaller = m < local;
-            rank += smaller ? 1u : 0u;
-            below += (mc < my_cls) ? 1u : 0u;
-            frank += (mc == my_cls && smaller) ? 1u : 0u;
-            hist += 1ull << (8u * (mc & 7u));
+            rank += ((e & imask) < local) ? 1u : 0u;
+            diff |= (e >> kClsShift) ^ my_cls;
+        }
+        if (grouped && diff) {  // several classes: the class histogram and my place in the walk copy
+            mixed = true;
+            hist = 0;
+            for (uint32_t t = st; t < en; ++t) {
+                const uint32_t e = __ldg(a.tmp + t);
+                const uint32_t mc = e >> kClsShift;
+                below += (mc < my_cls) ? 1u : 0u;
+                frank += (mc == my_cls && (e & imask) < local) ? 1u : 0u;
+                hist += 1ull << (8u * mc);
+            }
         }
     } else {
         rank = a.slot[i];
@@ -603,7 +612,6 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     // particle data in sorted order (coalesced writes, as the reference's
     // reorderDataCUDA gathers).  Buckets holding more than one alias class
     // also place the particle in the class-grouped walk copy.
-    const bool mixed = grouped && ((hist >> (8u * my_cls)) & 0xFFull) != en - st;
     a.wpos[g] = mixed ? d.p_off + (st - base) + below + frank : kNoWalkCopy;
     if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
     a.perm[g] = local;
