@@ -886,8 +886,10 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
     }
     const float mr = d.m * d.inv_rho0;
     const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
-    // |omega| once per particle in .w: pass 2 needs it for every neighbour
-    a.w[i] = make_float4(wi.x, wi.y, wi.z, sqrtf(wi.x * wi.x + wi.y * wi.y + wi.z * wi.z));
+    a.w[i] = wi;
+    // |omega| once per particle, beside the position (xs is free after the
+    // reorder): pass 2 gathers both with one load per neighbour
+    a.xs[i] = make_float4(xi.x, xi.y, xi.z, sqrtf(wi.x * wi.x + wi.y * wi.y + wi.z * wi.z));
     TILE_LOOP_END
 }
 
@@ -907,14 +909,15 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
     const float sgn = REF ? 1.f : -1.f;
     const float4 *__restrict__ x = a.x;
     const float4 *__restrict__ w = a.w;
+    const float4 *__restrict__ xw = a.xs;  // (x_j, |omega_j|), stored by pass 1
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
     auto use = [&](uint32_t j) {
-        const float4 xj = __ldg(x + j);
+        const float4 xj = __ldg(xw + j);
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
         const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
         if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
-            const float wl = __ldg(&w[j].w);  // |omega_j|, stored by pass 1
+            const float wl = xj.w;
             const float f = sgn * wl * wspiky_d(r2 * inv_r, kh) * inv_r;
             n0 += f * p0;
             n1 += f * p1;
