@@ -538,11 +538,44 @@ def main():
         pcells = int(np.prod(p["grid_size"])) + 1
         pbp, pbc = ALG_KERNEL.get(ptop, (0, 0))
         pach = (pbp * sc.n + pbc * pcells) / (statistics.mean(pprof[ptop]) / 1e3) / 1e9
+        per_kernel_gbps = {}
+        for name, ts in pprof.items():
+            kbp, kbc = ALG_KERNEL.get(name, (0, 0))
+            if kbp:
+                per_kernel_gbps[name] = round((kbp * sc.n + kbc * pcells) / (statistics.mean(ts) / 1e3) / 1e9, 1)
         single = {"value": sc.n / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
                   "workload": "single scene: 1,048,576 particles (128x128x64 dam break), 2^21-cell table, "
                               "plain step",
                   "top_kernel": ptop, "top_kernel_GBps": pach, "top_kernel_frac": pach / peak,
+                  "kernel_alg_GBps": per_kernel_gbps,
                   "step_alg_GBps": (ALG_STEP_P * sc.n + ALG_STEP_C * pcells) / (pms / 1e3) / 1e9}
+
+    # ---------------- config 1: the plain 32,768-particle dam break ----------------
+    small = None
+    if not args.no_plain and rank == 0:
+        from ssf_pbf_cuda_gb300 import scenes
+        sc = scenes.config1()
+        p = scene_params(sc)
+        part = api.PbfParticle(p, sc.n, sc.domain_end, device=local)
+        b = api.Boundary(points_on_planes=sc.planes[0], normals_on_planes=sc.planes[1])
+        xd = torch.from_numpy(sc.x).to(dev)
+        vd = torch.from_numpy(sc.v).to(dev)
+        for _ in range(args.warmup):
+            part.set_particles(xd, vd, stream)
+            api.one_step(part, b, sc.area, ITERS, stream)
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 100
+        c0.record(stream)
+        for _ in range(reps):
+            part.set_particles(xd, vd, stream)
+            api.one_step(part, b, sc.area, ITERS, stream)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        cms = c0.elapsed_time(c1) / reps
+        small = {"value": sc.n / (cms / 1e3), "unit": UNIT, "ms_per_step": cms,
+                 "workload": "plain dam break: 32,768 particles (32x32x32), 4 x 2 x 2 m box, 100 steps, "
+                             "each from the seeded initial state; launch / latency bound (L2-resident)"}
 
     # ---------------- serving: Poisson arrivals, continuous batching ----------------
     serving = None
@@ -566,6 +599,7 @@ def main():
             "config": dict(workload_config(len(scs), n_total, cells, world),
                            tile=tile, chunk=shape["chunk"]),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
+            "plain_dam_32k": small,
             "serving": serving, "ns_microbench": ns_micro,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
