@@ -32,7 +32,10 @@ def nvcc() -> str:
 
 
 def _flags(extra=()):
-    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-I", INCLUDE, "-I", CSRC,
+    # -ftz=true as the reference's shipped build (cuda_pbf_with_ssf.vcxproj:125-127);
+    # division and square root stay IEEE-rounded.  Positions and their
+    # differences are never subnormal, so the integer pipeline is unaffected.
+    return ["-O3", "-std=c++17", "-lineinfo", "-ftz=true", *ARCH, "-I", INCLUDE, "-I", CSRC,
             "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", *extra]
 
 
