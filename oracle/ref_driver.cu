@@ -14,6 +14,9 @@
 // Output: "PBFO", u32 num, u32 n_in, u32 grid[3], u32 max_pair, f32 x[3 num],
 //   v[3 num], u32 sorted_hash[n_in], sorted_index[n_in], cell_start[C],
 //   cell_end[C], neighbor_list[ceil32(num) * max_pair].
+// With a third argument R > 0 the step is first timed: R steps, each from
+// the input state (device-to-device reload inside the timed region), after
+// one warm-up step; "ms_per_step <t>" is printed to stdout.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -48,10 +51,11 @@ static void check(cudaError_t e, const char *what)
 
 int main(int argc, char **argv)
 {
-    if (argc != 3) {
-        fprintf(stderr, "usage: %s input.bin output.bin\n", argv[0]);
+    if (argc != 3 && argc != 4) {
+        fprintf(stderr, "usage: %s input.bin output.bin [timed_steps]\n", argv[0]);
         return 1;
     }
+    const int reps = argc == 4 ? atoi(argv[3]) : 0;
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 1;
     char magic[4];
@@ -100,21 +104,52 @@ int main(int argc, char **argv)
     pbf_buffer buf;
     buf.allocate(cap, part.ns->getMaxPairParticleNum());
     const std::pair<dom_dim, dom_dim> area(dom_dim(amin[0], amin[1], amin[2]), dom_dim(amax[0], amax[1], amax[2]));
-    if (use_b) {
-        std::vector<glm::vec4> in, out;
-        std::vector<dom_dim> pp, pn;
-        for (uint32_t k = 0; k < ni; ++k) in.emplace_back(inner[4 * k], inner[4 * k + 1], inner[4 * k + 2], inner[4 * k + 3]);
-        for (uint32_t k = 0; k < no; ++k) out.emplace_back(outer[4 * k], outer[4 * k + 1], outer[4 * k + 2], outer[4 * k + 3]);
-        for (uint32_t k = 0; k < np; ++k) {
-            pp.emplace_back(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]);
-            pn.emplace_back(nrm[3 * k], nrm[3 * k + 1], nrm[3 * k + 2]);
-        }
-        pbf_boundary bnd;
-        bnd.allocate(in, out, pp, pn);
-        pbf::one_step(part, buf, bnd, area, iters);
-    } else {
-        pbf::one_step(part, buf, area, iters);
+    std::vector<glm::vec4> in, out;
+    std::vector<dom_dim> pp, pn;
+    for (uint32_t k = 0; k < ni; ++k) in.emplace_back(inner[4 * k], inner[4 * k + 1], inner[4 * k + 2], inner[4 * k + 3]);
+    for (uint32_t k = 0; k < no; ++k) out.emplace_back(outer[4 * k], outer[4 * k + 1], outer[4 * k + 2], outer[4 * k + 3]);
+    for (uint32_t k = 0; k < np; ++k) {
+        pp.emplace_back(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]);
+        pn.emplace_back(nrm[3 * k], nrm[3 * k + 1], nrm[3 * k + 2]);
     }
+    pbf_boundary bnd;
+    if (use_b) bnd.allocate(in, out, pp, pn);
+    auto step = [&]() {
+        if (use_b) pbf::one_step(part, buf, bnd, area, iters);
+        else pbf::one_step(part, buf, area, iters);
+    };
+    if (reps > 0) {
+        float *x0 = nullptr, *v0 = nullptr;
+        check(cudaMalloc(&x0, 12ull * n), "x0");
+        check(cudaMalloc(&v0, 12ull * n), "v0");
+        check(cudaMemcpy(x0, part.phase.x, 12ull * n, cudaMemcpyDeviceToDevice), "x0 copy");
+        check(cudaMemcpy(v0, part.phase.v, 12ull * n, cudaMemcpyDeviceToDevice), "v0 copy");
+        auto reload = [&]() {
+            check(cudaMemcpy(part.phase.x, x0, 12ull * n, cudaMemcpyDeviceToDevice), "reload x");
+            check(cudaMemcpy(part.phase.v, v0, 12ull * n, cudaMemcpyDeviceToDevice), "reload v");
+            part.phase.num = n;
+        };
+        reload();
+        step();
+        check(cudaDeviceSynchronize(), "warm-up step");
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0);
+        for (int r = 0; r < reps; ++r) {
+            reload();
+            step();
+        }
+        cudaEventRecord(e1);
+        check(cudaEventSynchronize(e1), "timed steps");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        printf("ms_per_step %.6f\n", ms / reps);
+        reload();
+        cudaFree(x0);
+        cudaFree(v0);
+    }
+    step();
     check(cudaDeviceSynchronize(), "one_step");
 
     pbf::neighbor_search &ns = *part.ns;
