@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 
 import os
 import statistics
@@ -191,35 +192,49 @@ def run_serving(api, args, device: int) -> dict:
     import numpy as np
 
     from ssf_pbf_cuda_gb300 import scenes
-    rate = args.serve_rate
+
+    def serve(reqs):
+        tot_p = sum(sc.n for _, sc, _ in reqs)
+        cells = 0
+        plist = []
+        for _, sc, _ in reqs:
+            p = sc.params(api.config_params(scorr_k=1e-4))
+            p["grid_size"] = list(api.resolve_grid(p, sc.domain_end))
+            plist.append(p)
+            cells += int(np.prod(p["grid_size"])) + 1
+        srv = api.Server(hbm_budget_bytes=150 * 10 ** 9, max_scenes=len(reqs), max_particles=tot_p,
+                         max_cells=cells, iters=ITERS, device=device, tile=args.serve_tile)
+        srv.start()
+        t0 = time.perf_counter()
+        for (t_arr, sc, hz), p in zip(reqs, plist):
+            wait = t_arr - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            srv.submit(p, sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes)
+        srv.stop(drain=True)
+        wall = time.perf_counter() - t0
+        comps = srv.poll(len(reqs) + 16)
+        st = srv.stats()
+        del srv
+        return comps, st, wall
+
+    # the rate that saturates the device: the server's busy throughput on a
+    # burst of requests (all queued at once) over the mean work of a request,
+    # E[N] E[horizon] with N log-uniform in [8192, 262144], horizon uniform in
+    # [60, 600]
+    mean_n = (262144 - 8192) / math.log(262144 / 8192)
+    mean_work = mean_n * (60 + 600) / 2
+    _, st_cal, _ = serve(scenes.config5_requests(24, 1e6, seed_id=55))
+    busy_tp = st_cal["particle_steps"] / max(st_cal["busy_s"], 1e-9)
+    rate = args.serve_rate if args.serve_rate > 0 else busy_tp / mean_work
     n_req = max(1, int(rate * args.serve_seconds))
-    reqs = scenes.config5_requests(n_req, rate)
-    tot_p = sum(sc.n for _, sc, _ in reqs)
-    cells = 0
-    plist = []
-    for _, sc, _ in reqs:
-        p = sc.params(api.config_params(scorr_k=1e-4))
-        p["grid_size"] = list(api.resolve_grid(p, sc.domain_end))
-        plist.append(p)
-        cells += int(np.prod(p["grid_size"])) + 1
-    srv = api.Server(hbm_budget_bytes=150 * 10 ** 9, max_scenes=len(reqs), max_particles=tot_p,
-                     max_cells=cells, iters=ITERS, device=device, tile=args.serve_tile)
-    srv.start()
-    t0 = time.perf_counter()
-    rids = []
-    for (t_arr, sc, hz), p in zip(reqs, plist):
-        wait = t_arr - (time.perf_counter() - t0)
-        if wait > 0:
-            time.sleep(wait)
-        rids.append(srv.submit(p, sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes))
-    srv.stop(drain=True)
-    wall = time.perf_counter() - t0
-    comps = srv.poll(len(reqs) + 16)
-    st = srv.stats()
+    comps, st, wall = serve(scenes.config5_requests(n_req, rate))
     lat = np.array(sorted(c["complete_s"] - c["arrival_s"] for c in comps))
     qd = np.array(sorted(c["admit_s"] - c["arrival_s"] for c in comps))
     return {
         "requests": len(comps), "arrival_rate_hz": rate, "arrival_window_s": args.serve_seconds,
+        "rate_rule": "saturating: burst busy throughput / mean request work" if args.serve_rate <= 0 else "fixed",
+        "burst_busy_particle_steps_per_s": busy_tp,
         "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
         "p99_queue_s": float(np.percentile(qd, 99)),
         "particle_steps_per_s": st["particle_steps"] / wall, "busy_particle_steps_per_s":
@@ -336,7 +351,8 @@ def main():
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
     ap.add_argument("--chunk", type=int, default=0, help="neighbour chunk of the lambda/dp passes (0 = autotune)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="arrival window of the serving run (0 = off)")
-    ap.add_argument("--serve-rate", type=float, default=12.0, help="request arrivals per second")
+    ap.add_argument("--serve-rate", type=float, default=0.0,
+                    help="request arrivals per second (0 = the rate that saturates the device)")
     ap.add_argument("--serve-tile", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
