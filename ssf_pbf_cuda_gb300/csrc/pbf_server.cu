@@ -5,7 +5,11 @@
 // and the arena allow, advances every resident scene by one step per
 // substep (one batched launch sequence), and evicts a scene when it reaches
 // its horizon or reports non-finite positions.  New requests join between
-// substeps, so work from different requests overlaps on the device.
+// substeps, so work from different requests overlaps on the device.  When no
+// resident scene reaches its horizon sooner, up to kMaxBurst steps run back
+// to back between host checks (the device-side flags accumulate), so the
+// host round trip is paid once per burst.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -21,6 +25,8 @@
 using namespace pbf103;
 
 namespace {
+constexpr uint32_t kMaxBurst = 8;
+
 struct Request {
     uint64_t id = 0;
     pbf_request_desc desc{};
@@ -115,9 +121,15 @@ pbf_status pbf_server::service(bool *did_work)
     }
     if (resident.empty()) return PBF_SUCCESS;
 
+    // steps until the first resident scene reaches its horizon, at most kMaxBurst
+    uint32_t burst = kMaxBurst;
+    for (Request *r : resident) burst = std::min(burst, r->desc.horizon_steps - r->steps);
+    burst = std::max(burst, 1u);
     const double t_step = now();
-    pbf_status rc = batch.step(cfg.iters, stream);
-    if (rc != PBF_SUCCESS) return rc;
+    for (uint32_t k = 0; k < burst; ++k) {
+        pbf_status rc = batch.step(cfg.iters, stream);
+        if (rc != PBF_SUCCESS) return rc;
+    }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return PBF_ERROR_CUDA;
     const double t_done = now();
     *did_work = true;
@@ -125,12 +137,12 @@ pbf_status pbf_server::service(bool *did_work)
     std::vector<Request *> keep;
     keep.reserve(resident.size());
     uint64_t ps = 0;
-    rc = batch.read_all(nums, flags, true, stream);
+    pbf_status rc = batch.read_all(nums, flags, true, stream);
     if (rc != PBF_SUCCESS) return rc;
     for (Request *r : resident) {
         const uint32_t n = nums[r->scene], f = flags[r->scene];
-        ps += n;
-        r->steps++;
+        ps += (uint64_t)n * burst;  // live count after the burst (deletions only lower it)
+        r->steps += burst;
         r->flags |= f;
         const bool finished = r->steps >= r->desc.horizon_steps || (f & PBF_FLAG_NONFINITE);
         if (!finished) {
@@ -153,7 +165,7 @@ pbf_status pbf_server::service(bool *did_work)
     }
     std::lock_guard<std::mutex> lk(mu);
     resident.swap(keep);
-    st.substeps++;
+    st.substeps += burst;
     st.particle_steps += ps;
     st.busy_s += t_done - t_step;
     return PBF_SUCCESS;
