@@ -81,13 +81,11 @@ __device__ __forceinline__ PairK pair_kernel(float4 xi, float4 xj, float inv_h, 
     const float r = r2 * inv_r;
     const float u = fmaf(-r, inv_h, 1.f);
     const float kd = (inv_h <= inv_r) ? beta * u * u : 0.f;
-    o.gx = o.gy = o.gz = 0.f;
-    if (r2 > 0.f) {
-        const float s = kd * inv_r;
-        o.gx = s * d0;
-        o.gy = s * d1;
-        o.gz = s * d2;
-    }
+    // grad W = 0 for the pair with itself (r2 = 0, where kd and inv_r are not finite)
+    const float s = (r2 > 0.f) ? kd * inv_r : 0.f;
+    o.gx = s * d0;
+    o.gy = s * d1;
+    o.gz = s * d2;
     return o;
 }
 
