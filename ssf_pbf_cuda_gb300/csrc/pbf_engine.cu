@@ -1031,9 +1031,9 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
         chunk_ = ch;
         rc = upload(st);
         if (rc != PBF_SUCCESS) break;
-        run(iters, st, false);  // warm-up
+        for (int r = 0; r < 2; ++r) run(iters, st, false);  // warm-up
         CK(cudaEventRecord(e0, st));
-        for (int r = 0; r < 3; ++r) run(iters, st, false);
+        for (int r = 0; r < 8; ++r) run(iters, st, false);
         CK(cudaEventRecord(e1, st));
         CK(cudaEventSynchronize(e1));
         float ms = 0;
