@@ -194,62 +194,29 @@ __device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, floa
 // pbf_neighbor_search_util.cu:428-452), as contiguous sorted-index ranges:
 // r(st, en) gets [st, en) and returns false to stop the walk.  When the
 // three x-cells of a row are consecutive hashes their particles form one
-// range.
-//
-// PRUNE restricts the walk to cells that can hold a particle within h of xp
-// (the binned position): a cell, or a whole row of three, whose nearest point
-// is farther than h holds no accepted candidate, so skipping it leaves the
-// visited sequence of accepted candidates unchanged.  A 1e-3 relative margin
-// covers the rounding of the cell assignment.  With fewer than 4 cells on an
-// axis the reference visits wrapped cells more than once; then every cell is
-// visited.  The rows and cells are one loop nest with a single call site of
-// r, so r's body is inlined once.
-template <bool PRUNE, class R>
+// range.  Every cell is visited (the reference-form XSPH and vorticity
+// walks); with fewer than 3 cells on an axis a wrapped cell is visited more
+// than once, as in the reference.
+template <class R>
 __device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t *__restrict__ offsets,
                                               uint32_t shift, float4 xp, R &&r)
 {
-    const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
-    const bool prune = PRUNE && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
-    float lx = 0.f, ly = 0.f, lz = 0.f, rx = 0.f, ry = 0.f, rz = 0.f;
-    if (prune) {
-        lx = xp.x - (float)icx * d.cw;
-        ly = xp.y - (float)icy * d.cw;
-        lz = xp.z - (float)icz * d.cw;
-        rx = d.cw - lx;
-        ry = d.cw - ly;
-        rz = d.cw - lz;
-    }
-    const float lim = d.h2 * 1.001f;
-    const uint32_t gx = (uint32_t)icx, gy = (uint32_t)icy, gz = (uint32_t)icz;
+    const uint32_t gx = (uint32_t)cell_coord(xp.x, d.cw), gy = (uint32_t)cell_coord(xp.y, d.cw),
+                   gz = (uint32_t)cell_coord(xp.z, d.cw);
     const uint32_t *off = offsets + d.c_off;
     const uint32_t mx = d.gx - 1u;
-    const uint32_t x0c = (gx - 1u) & mx, x1c = gx & mx, x2c = (gx + 1u) & mx;
+    const uint32_t x0c = (gx - 1u) & mx, x2c = (gx + 1u) & mx;
     const bool contiguous = (x2c == x0c + 2u);
 #pragma unroll 1
     for (int rr = 0; rr < 9; ++rr) {
         const int dz = rr / 3 - 1, dy = rr % 3 - 1;
-        bool left = true, right = true;
-        if (prune) {
-            const float ez = dz < 0 ? lz : (dz > 0 ? rz : 0.f);
-            const float ey = dy < 0 ? ly : (dy > 0 ? ry : 0.f);
-            const float eyz2 = ey * ey + ez * ez;
-            if (eyz2 > lim) continue;
-            left = eyz2 + lx * lx <= lim;
-            right = eyz2 + rx * rx <= lim;
-        }
         const uint32_t row = ((gz + (uint32_t)dz) & (d.gz - 1u)) * d.gx * d.gy +
                              ((gy + (uint32_t)dy) & (d.gy - 1u)) * d.gx;
         const uint32_t nseg = contiguous ? 1u : 3u;
 #pragma unroll 1
         for (uint32_t sg = 0; sg < nseg; ++sg) {
-            uint32_t lo, hi;
-            if (contiguous) {
-                lo = left ? x0c : x1c;
-                hi = right ? x2c : x1c;
-            } else {
-                if ((sg == 0 && !left) || (sg == 2 && !right)) continue;
-                lo = hi = (gx + sg - 1u) & mx;
-            }
+            const uint32_t lo = contiguous ? x0c : (gx + sg - 1u) & mx;
+            const uint32_t hi = contiguous ? x2c : lo;
             if (!r(__ldg(off + row + lo) + shift, __ldg(off + row + hi + 1u) + shift)) return;
         }
     }
@@ -266,7 +233,14 @@ __device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t
 // accepted sequence is the reference's.  Buckets marked kClassWhole (and
 // every bucket of a scene with an axis of fewer than 4 cells, where the
 // reference visits wrapped cells twice) are visited whole, in sorted order.
-// r(src, st, en) gets the array and the range.  PRUNE as in walk27_ranges.
+// r(src, st, en) gets the array and the range.
+//
+// PRUNE restricts the walk to cells that can hold a particle within h of xp
+// (the binned position): a cell whose nearest point is farther than h holds
+// no accepted candidate, so skipping it leaves the visited sequence of
+// accepted candidates unchanged.  A 1e-3 relative margin covers the rounding
+// of the cell assignment.  It applies only when every axis has at least 4
+// cells (with fewer, the reference visits wrapped cells more than once).
 template <bool PRUNE, class R>
 __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t *__restrict__ offsets,
                                              const uint64_t *__restrict__ chist, const float4 *xa,
@@ -339,7 +313,7 @@ __device__ __forceinline__ void walk27_batched(const SceneDesc &d, const uint32_
     constexpr int kBuf = 32;
     uint32_t buf[kBuf];
     int nb = 0;
-    walk27_ranges<false>(d, offsets, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
+    walk27_ranges(d, offsets, shift, xp, [&](uint32_t st, uint32_t en) -> bool {
         for (uint32_t j = st; j < en; ++j) {
             if (accept(j)) {
                 buf[nb++] = j;
