@@ -178,7 +178,7 @@ Batch::~Batch()
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
                     d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
-                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_xv_};
+                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_xv_, d_dense_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -225,6 +225,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_nnb_, P));
     CK(A((void **)&d_cls_, P));
     CK(A((void **)&d_xv_, 32 * P));
+    CK(A((void **)&d_dense_, 4 * (2 * (P / 64 + 1) + 1)));  // a dense bucket holds more than 64 particles
     CK(A((void **)&d_chist_, 8 * (C + 4)));
     CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
     CK(A((void **)&d_pack_off_, 4ull * max_scenes));
@@ -668,6 +669,7 @@ StepArgs Batch::args() const
     a.wx = d_wx_;
     a.wpos = d_wpos_;
     a.xv = d_xv_;
+    a.dense = d_dense_;
     a.chist = d_chist_;
     a.id_tmp = d_id_tmp_;
     a.next_id = d_next_id_;

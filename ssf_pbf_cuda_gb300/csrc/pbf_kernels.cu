@@ -448,7 +448,10 @@ __global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
     const uint32_t n = a.ctrl->n_cells;
     const uint32_t ntile = (n + kScanTile - 1) / kScanTile;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        *a.dense = 0;  // the dense-bucket queue of this step's k_rank_reorder
+    }
     __syncthreads();
     for (uint32_t base = 0; base < ntile; base += 1024) {
         const uint32_t idx = base + threadIdx.x;
@@ -536,6 +539,10 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
 // kStableLimit keep the atomic order (PBF_FLAG_UNSTABLE_ORDER is not part of
 // the ABI; such buckets only arise from degenerate inputs or mass deletion).
 constexpr uint32_t kStableLimit = 4096;
+// Buckets with more members than kDenseMin (and at most kStableLimit) are
+// ordered by k_dense_sort (a block per bucket) instead of a member scan per
+// particle, which costs O(members^2) per bucket.
+constexpr uint32_t kDenseMin = 64;
 
 __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
 {
@@ -556,6 +563,16 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
     uint64_t hist = (uint64_t)(en - st) << (8u * my_cls);  // every member of my class
     bool mixed = false;
+    if (en - st > kDenseMin && en - st <= kStableLimit) {
+        // a dense bucket: one block of k_dense_sort orders it; its first
+        // member by atomic slot queues it
+        if (a.slot[i] == 0) {
+            const uint32_t k = atomicAdd(a.dense, 1u);
+            a.dense[1 + 2 * k] = gk;
+            a.dense[2 + 2 * k] = s;
+        }
+        continue;
+    }
     if (en - st <= kStableLimit) {
         rank = 0;
         uint32_t diff = 0;
@@ -588,6 +605,92 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
     a.perm[g] = local;
     TILE_LOOP_END
+}
+
+// Dense buckets queued by k_rank_reorder, one block each: the members'
+// bucket entries (input index, alias class in the top bits) are sorted in
+// shared memory by input index (the stable sorted order) and, when the
+// bucket mixes classes, by (class, index) (the walk copy's order); the
+// results are the same permutation, class counts and walk-copy places the
+// per-particle member scan of k_rank_reorder produces.
+__device__ __forceinline__ uint32_t dense_key(uint32_t e, uint32_t imask)
+{
+    return e == 0xFFFFFFFFu ? 0xFFFFFFFFu : (e & imask);  // padding sorts last
+}
+
+template <bool FULL>
+__device__ void bitonic_sort(uint32_t *v, uint32_t n, uint32_t imask)
+{
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+                const uint32_t i = 2 * stride * (t / stride) + (t % stride), j = i + stride;
+                const uint32_t vi = v[i], vj = v[j];
+                const uint32_t ki = FULL ? vi : dense_key(vi, imask), kj = FULL ? vj : dense_key(vj, imask);
+                const bool asc = (i & size) == 0;
+                if ((ki > kj) == asc) {
+                    v[i] = vj;
+                    v[j] = vi;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dense_sort(StepArgs a)
+{
+    __shared__ uint32_t S[kStableLimit], W[kStableLimit];
+    __shared__ uint32_t chist_cnt[8];
+    const uint32_t nd = *(volatile const uint32_t *)a.dense;
+    for (uint32_t k = blockIdx.x; k < nd; k += gridDim.x) {
+        const uint32_t gk = a.dense[1 + 2 * k], s = a.dense[2 + 2 * k];
+        const SceneDesc &d = a.scenes[s];
+        const uint32_t st = a.offsets[gk], en = a.offsets[gk + 1], b = en - st;
+        const uint32_t base = a.offsets[d.c_off];
+        const uint32_t g0 = d.p_off + (st - base);
+        const bool packed = d.capacity <= kClsLimit;
+        const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
+        const bool grouped = packed && b <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+        uint32_t P = 1;
+        while (P < b) P <<= 1;
+        if (threadIdx.x < 8) chist_cnt[threadIdx.x] = 0;
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
+            const uint32_t e = t < b ? a.tmp[st + t] : 0xFFFFFFFFu;
+            S[t] = e;
+            W[t] = e;
+            if (t < b && grouped) atomicAdd(&chist_cnt[e >> kClsShift], 1u);
+        }
+        __syncthreads();
+        bitonic_sort<false>(S, P, imask);
+        uint64_t hist = 0;
+        uint32_t classes = 0;
+        for (uint32_t c = 0; c < 8; ++c) {
+            hist |= (uint64_t)chist_cnt[c] << (8u * c);
+            classes += chist_cnt[c] ? 1u : 0u;
+        }
+        const bool mixed = grouped && classes > 1;
+        if (mixed) bitonic_sort<true>(W, P, imask);  // (class, index) order
+        for (uint32_t t = threadIdx.x; t < b; t += blockDim.x) {
+            a.perm[g0 + t] = S[t] & imask;
+            if (!mixed) a.wpos[g0 + t] = kNoWalkCopy;
+        }
+        if (mixed) {
+            for (uint32_t w = threadIdx.x; w < b; w += blockDim.x) {
+                const uint32_t key = W[w] & imask;  // its place in S (sorted by index)
+                uint32_t lo = 0, hi = b;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if ((S[mid] & imask) < key) lo = mid + 1;
+                    else hi = mid;
+                }
+                a.wpos[g0 + lo] = g0 + w;
+            }
+        }
+        if (threadIdx.x == 0) a.chist[gk] = grouped ? hist : kClassWhole;
+        __syncthreads();
+    }
 }
 
 // Reorder in sorted order (reorderDataCUDA x2, pbf_neighbor_search_util.cu:143-154):
@@ -1165,6 +1268,8 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     PBF_LAUNCHED("k_scatter");
     k_rank_reorder<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_rank_reorder");
+    k_dense_sort<<<sh.grid, 256, 0, st>>>(a);
+    PBF_LAUNCHED("k_dense_sort");
     k_gather<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_gather");
     k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
