@@ -93,7 +93,7 @@ struct StepArgs {
 struct LaunchShape {
     uint32_t tile;        // particles per tile = threads per block
     uint32_t grid;        // persistent grid (blocks) for the light tile kernels
-    uint32_t scan_grid;   // grid for the scan kernels
+    uint32_t scan_grid;   // grid for the scan kernels; 0 = the one-block scan
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
@@ -152,5 +152,6 @@ constexpr uint64_t kClassWhole = ~0ull;
 constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;
 constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells per scan tile
+constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
 
 }  // namespace pbf103

@@ -473,6 +473,42 @@ __global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
     if (threadIdx.x == 0) a.offsets[n] = carry;
 }
 
+// The whole scan in one block, for tables of at most kSingleScanMax cells
+// (small scenes: one launch instead of three).
+__global__ void __launch_bounds__(1024) k_scan_single(StepArgs a)
+{
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    const uint32_t n = a.ctrl->n_cells;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        *a.dense = 0;  // the dense-bucket queue of this step's k_rank_reorder
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += 1024) {
+        const uint32_t idx = base + threadIdx.x;
+        const uint32_t v = idx < n ? a.count[idx] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (lane == 31) ws[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t wv = ws[lane];
+            ws[lane] = warp_incl_scan(wv) - wv;
+        }
+        __syncthreads();
+        const uint32_t c = carry;
+        if (idx < n) {
+            a.offsets[idx] = c + ws[warp] + inc - v;
+            a.count[idx] = 0u;  // ready for the next step's histogram
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + ws[warp] + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.offsets[n] = carry;
+}
+
 __global__ void __launch_bounds__(256) k_scan_down(StepArgs a)
 {
     __shared__ uint32_t ws[kScanWarps];
@@ -1258,12 +1294,17 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     } while (0)
     k_predict_hash<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_predict_hash");
-    k_scan_reduce<<<sh.scan_grid, 256, 0, st>>>(a);
-    PBF_LAUNCHED("k_scan_reduce");
-    k_scan_spine<<<1, 1024, 0, st>>>(a);
-    PBF_LAUNCHED("k_scan_spine");
-    k_scan_down<<<sh.scan_grid, 256, 0, st>>>(a);
-    PBF_LAUNCHED("k_scan_down");
+    if (sh.scan_grid == 0) {  // small table: one block
+        k_scan_single<<<1, 1024, 0, st>>>(a);
+        PBF_LAUNCHED("k_scan_single");
+    } else {
+        k_scan_reduce<<<sh.scan_grid, 256, 0, st>>>(a);
+        PBF_LAUNCHED("k_scan_reduce");
+        k_scan_spine<<<1, 1024, 0, st>>>(a);
+        PBF_LAUNCHED("k_scan_spine");
+        k_scan_down<<<sh.scan_grid, 256, 0, st>>>(a);
+        PBF_LAUNCHED("k_scan_down");
+    }
     k_scatter<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_scatter");
     k_rank_reorder<<<g, b, 0, st>>>(a);
