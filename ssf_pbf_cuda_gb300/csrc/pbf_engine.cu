@@ -163,9 +163,8 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
 
 uint64_t bytes_per_particle(uint32_t max_pair)
 {
-    // x v xs xa xb xold w vt wx (float4) + xv (2 float4) + key slot tmp perm id id_tmp wpos + lam + nnb + cls
-    // + nbr
-    return 11 * 16 + 7 * 4 + 4 + 1 + 1 + 4ull * (max_pair - 1);
+    // x v xs xa xb xold w vt wx (float4) + key slot tmp perm id id_tmp wpos + lam + nnb + cls + nbr
+    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 4ull * (max_pair - 1);
 }
 
 // ---------------------------------------------------------------- batch --
@@ -178,7 +177,7 @@ Batch::~Batch()
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
                     d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
-                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_xv_, d_dense_};
+                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -224,7 +223,6 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_nbr_, 4ull * (max_pair - 1) * P));
     CK(A((void **)&d_nnb_, P));
     CK(A((void **)&d_cls_, P));
-    CK(A((void **)&d_xv_, 32 * P));
     CK(A((void **)&d_dense_, 4 * (2 * (P / 64 + 1) + 1)));  // a dense bucket holds more than 64 particles
     CK(A((void **)&d_chist_, 8 * (C + 4)));
     CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
@@ -669,7 +667,6 @@ StepArgs Batch::args() const
     a.cls = d_cls_;
     a.wx = d_wx_;
     a.wpos = d_wpos_;
-    a.xv = d_xv_;
     a.dense = d_dense_;
     a.chist = d_chist_;
     a.id_tmp = d_id_tmp_;

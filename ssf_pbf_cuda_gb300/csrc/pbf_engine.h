@@ -141,7 +141,6 @@ private:
     float4 *d_wx_ = nullptr;                          // class-grouped walk copy of the sorted positions
     uint64_t *d_chist_ = nullptr;                     // per cell: class counts of its bucket
     uint32_t *d_wpos_ = nullptr;                      // sorted slot -> walk-copy slot
-    float4 *d_xv_ = nullptr;                          // interleaved final position / velocity
     uint32_t *d_dense_ = nullptr;                     // dense-bucket queue
     uint32_t *h_small_ = nullptr;     // pinned host scratch: pack offsets + counts
     cudaEvent_t small_done_ = nullptr;

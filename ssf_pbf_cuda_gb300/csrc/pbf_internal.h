@@ -82,7 +82,6 @@ struct StepArgs {
     uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
     uint8_t *cls;                 // alias class of each particle (input order)
     uint32_t *wpos;               // sorted slot -> walk-copy slot (mixed-class buckets only)
-    float4 *xv;                   // [2i] final position, [2i+1] velocity: the post passes' gathers (or null)
     uint32_t *dense;              // [0] count, then (cell, scene) pairs of buckets for k_dense_sort
     float4 *wx;                   // walk copy of mixed-class buckets: grouped by class, .w = sorted slot
     uint64_t *chist;              // per cell: 8 x 8-bit class counts of its bucket, or kClassWhole

@@ -925,14 +925,8 @@ __global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restr
     xo[i] = xn;
     if (last) {
         const float4 xo_ = a.xold[i];
-        const float4 vn =
-            make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
-        vo[i] = vn;
+        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
         a.id[i] = a.id_tmp[i];  // ids follow the particles into sorted order
-        if (a.xv) {  // position and velocity side by side for the post passes' neighbour gathers
-            a.xv[2ull * i] = xn;
-            a.xv[2ull * i + 1] = vn;
-        }
     }
     TILE_LOOP_END
 }
@@ -950,13 +944,8 @@ __global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict
     const float4 xn = a.xa[i];
     const float4 xo_ = a.xold[i];
     a.x[i] = xn;
-    const float4 vn = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
-    vo[i] = vn;
+    vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
     a.id[i] = a.id_tmp[i];
-    if (a.xv) {
-        a.xv[2ull * i] = xn;
-        a.xv[2ull * i + 1] = vn;
-    }
     TILE_LOOP_END
 }
 
@@ -979,16 +968,14 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
     const float4 xi = a.x[i], vi = vs[i];
     const float kh = REF ? d.h : d.inv_h;
     const float4 *__restrict__ x = a.x;
-    const float4 *__restrict__ xv = a.xv;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
     auto use = [&](uint32_t j) {
-        // list form: position and velocity from one 32-byte record
-        const float4 xj = REF ? __ldg(x + j) : __ldg(xv + 2ull * j);
-        const float4 vj = REF ? __ldg(vs + j) : __ldg(xv + 2ull * j + 1);
+        const float4 xj = __ldg(x + j);
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
         const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
         if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
+            const float4 vj = __ldg(vs + j);
             const float v0 = vj.x - vi.x, v1 = vj.y - vi.y, v2 = vj.z - vi.z;
             const float wd = wspiky_d(r2 * inv_r, kh) * inv_r;
             w0 += (v1 * p2 - v2 * p1) * wd;
@@ -1087,7 +1074,6 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
         }
     }
     vs[i] = v;
-    if (a.xv) a.xv[2ull * i + 1] = v;
     TILE_LOOP_END
 }
 
@@ -1112,19 +1098,17 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
     }
     const float inv_h = d.inv_h, alpha6 = d.alpha6;
     const float4 *__restrict__ x = a.x;
-    const float4 *__restrict__ xv = a.xv;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     const float ih2 = inv_h * inv_h;
     auto use = [&](uint32_t j) {
-        // list form: position and velocity from one 32-byte record
-        const float4 xj = WALK ? __ldg(x + j) : __ldg(xv + 2ull * j);
+        const float4 xj = __ldg(x + j);
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
         // Wpoly6 from r^2 (q^2 = r^2 / h^2 instead of (|r| / h)^2: no square
         // root per pair; the two differ by rounding only)
         const float q2 = (p0 * p0 + p1 * p1 + p2 * p2) * ih2;
         const float t = 1.f - q2;
         const float W = (q2 <= 1.f) ? alpha6 * t * t * t : 0.f;
-        const float4 vj = WALK ? __ldg(vs + j) : __ldg(xv + 2ull * j + 1);
+        const float4 vj = __ldg(vs + j);
         s0 += (vj.x - vi.x) * W;
         s1 += (vj.y - vi.y) * W;
         s2 += (vj.z - vi.z) * W;
@@ -1316,51 +1300,49 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
     PBF_LAUNCHED("k_neighbors_lambda");
     const bool xsph = (post & (kPostXsphWalk | kPostXsphList)) != 0;
-    StepArgs ax = a;  // the last delta-p pass fills xv only when a list-form post pass reads it
-    if (!(post & (kPostXsphList | kPostVortTextbook))) ax.xv = nullptr;
     float4 *vfinal = xsph ? a.vt : a.v;
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            PBF_PASS_DISPATCH(sh.chunk, launch_lambda(ax, sh, cur, st));
+            PBF_PASS_DISPATCH(sh.chunk, launch_lambda(a, sh, cur, st));
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        PBF_PASS_DISPATCH(sh.chunk, launch_dp(ax, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
+        PBF_PASS_DISPATCH(sh.chunk, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;
         nxt = t;
     }
     if (iters <= 0) {
-        k_finalize<<<g, b, 0, st>>>(ax, vfinal);
+        k_finalize<<<g, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_finalize");
     }
     // omega of every form before any apply: both forms read final positions
     // and velocities only
     if (post & kPostVortTextbook) {
-        k_vort_omega<false><<<sh.grid_omega, b, 0, st>>>(ax, vfinal);
+        k_vort_omega<false><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega");
     }
     if (post & kPostVortReference) {
-        k_vort_omega<true><<<sh.grid_omega, b, 0, st>>>(ax, vfinal);
+        k_vort_omega<true><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega_walk");
     }
     if (post & kPostVortTextbook) {
-        k_vort_apply<false><<<sh.grid_apply, b, 0, st>>>(ax, vfinal);
+        k_vort_apply<false><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply");
     }
     if (post & kPostVortReference) {
-        k_vort_apply<true><<<sh.grid_apply, b, 0, st>>>(ax, vfinal);
+        k_vort_apply<true><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply_walk");
     }
     if (post & kPostXsphList) {
-        k_xsph<false><<<sh.grid_xsph, b, 0, st>>>(ax, a.vt, a.v);
+        k_xsph<false><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph");
     }
     if (post & kPostXsphWalk) {
-        k_xsph<true><<<sh.grid_xsph, b, 0, st>>>(ax, a.vt, a.v);
+        k_xsph<true><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph_walk");
     }
 #undef PBF_LAUNCHED
