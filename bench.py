@@ -281,6 +281,59 @@ def run_ns_microbench(api, device: int, reps: int = 3) -> dict:
     return out
 
 
+def ssf_alg_bytes(w: int, h: int, n: int, blur_passes: int) -> int:
+    """Algorithmic bytes of one screen-space frame: clear 4 B/pixel, each
+    blur pass 4 in + 4 out, normals 4 in + 16 out, shading 4 + 16 in and
+    16 + 4 out; 12 B per particle position read by the splat."""
+    return (4 + 8 * blur_passes + 20 + 40) * w * h + 12 * n
+
+
+def run_ssf_bench(api, torch, device: int, with_cpu: bool, frames: int = 200) -> dict:
+    """Headless screen-space fluid frames (depth splat, blur x3, normals,
+    shading), timed with CUDA events on the launching stream: the reference's
+    own frame (1280 x 720, its first-frame camera) of the 32,768-particle dam
+    break, and the 1,048,576-particle lattice at 1920 x 1080.  The CPU
+    baseline is the oracle's frame (one thread)."""
+    import numpy as np
+
+    from ssf_pbf_cuda_gb300 import scenes
+    out = {}
+    stream = torch.cuda.Stream(device)
+    peak, _ = measured_peak_hbm()
+    cases = [("dam_32k_720p", scenes.config1().x, 1280, 720), ("lattice_1m_1080p", scenes.config2().x, 1920, 1080)]
+    for name, x, w, h in cases:
+        r = api.SsfRenderer(width=w, height=h, device=device)
+        xd = torch.from_numpy(x).to(f"cuda:{device}")
+        with torch.cuda.stream(stream):
+            for _ in range(5):
+                r.render(xd, stream)
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(frames):
+                r.render(xd, stream)
+            e1.record(stream)
+            stream.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        alg = ssf_alg_bytes(w, h, len(x), r.params["blur_passes"])
+        case = {"particles": len(x), "width": w, "height": h, "ms_per_frame": ms, "frames_per_s": 1e3 / ms,
+                "launches_per_frame": r.launches, "alg_GBps": alg / (ms / 1e3) / 1e9,
+                "frac_of_hbm_peak": alg / (ms / 1e3) / 1e9 / peak,
+                "l2": "images L2-resident" if 44 * w * h < 129e6 else "images exceed L2"}
+        if with_cpu and name == "dam_32k_720p":
+            from oracle import ssf as S  # the CPU baseline: the oracle's frame
+            inv, inc = r.frame_constants()
+            f = S.frame(r.params, inv, inc)
+            t0 = time.perf_counter()
+            S.render(f, x, r.params["blur_passes"])
+            cpu_ms = (time.perf_counter() - t0) * 1e3
+            case["cpu_baseline"] = {"ms_per_frame": cpu_ms, "cores": 1, "kind": "port",
+                                    "sample": "one whole frame of the same workload"}
+        out[name] = case
+        del r, xd
+    return out
+
+
 def workload_config(n_scenes: int, particles: int, cells: int, world: int) -> dict:
     """The batched workload as both arms name it."""
     return {"workload": f"batched: {n_scenes} dam-break scenes per GPU, 4k-64k particles "
@@ -348,6 +401,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ssf", action="store_true", help="skip the screen-space fluid frame timing")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
     ap.add_argument("--preheat", type=float, default=3.0,
                     help="seconds of untimed steps before the warm-up: a GPU coming out of idle runs the first "
@@ -634,6 +688,10 @@ def main():
     if rank == 0 and not args.no_plain:
         ns_micro = run_ns_microbench(api, local)
 
+    ssf = None
+    if rank == 0 and not args.no_ssf:
+        ssf = run_ssf_bench(api, torch, local, not args.no_cpu)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v_cpu, sample, cores = cpu_baseline_sample(scs, scene_params, 10.0)
@@ -648,7 +706,7 @@ def main():
                            tile=tile, chunk=shape["chunk"], preheat_s=args.preheat),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
             "plain_dam_32k": small,
-            "serving": serving, "ns_microbench": ns_micro,
+            "serving": serving, "ns_microbench": ns_micro, "ssf_frame": ssf,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
         }

@@ -328,6 +328,72 @@ pbf_status pbf_batch_generate(pbf_batch *b, uint32_t scene_id, const pbf_arrange
                               void *stream, uint32_t *n_points);
 pbf_status pbf_batch_emit(pbf_batch *b, uint32_t scene_id, const pbf_emitter *e, double max_fill, void *stream);
 
+/* ---- headless screen-space fluid rendering ----
+ * The reference's per-frame GL passes (src/main.cpp:372-564) as CUDA kernels
+ * writing device image buffers; no graphics API is involved.
+ *   depth splat: ssf_object.vert/.geom/.frag (the quad main.cpp draws,
+ *                main.cpp:372-393) or ssf_point_sprite.vert/.frag;
+ *   blur:        ssf_blur.frag, blur_passes times, ping-pong (main.cpp:430-509);
+ *   normals:     ssf_normal.frag on the last blurred depth (main.cpp:511-531);
+ *   shading:     ssf_shading.frag over the unblurred depth, blended
+ *                (SRC_ALPHA, ONE_MINUS_SRC_ALPHA) onto the clear colour
+ *                (main.cpp:541-564).
+ * Images are row-major with row 0 at the bottom (GL window coordinates). */
+#define PBF_SSF_SPLAT_QUAD 0    /* ssf_object: view-space quad of side point_radius */
+#define PBF_SSF_SPLAT_SPRITE 1  /* ssf_point_sprite: point of point_radius * point_scale / dist pixels */
+
+#define PBF_SSF_DEPTH 0         /* float [h][w], window depth in [0, 1], 1 = empty */
+#define PBF_SSF_BLURRED 1       /* float [h][w], the last blur pass's output */
+#define PBF_SSF_BLUR_INPUT 2    /* float [h][w], the last blur pass's input */
+#define PBF_SSF_NORMAL 3        /* float [h][w][4], eye-space normal, w = 1; empty pixels = clear colour */
+#define PBF_SSF_COLOR 4         /* float [h][w][4], shaded colour blended onto the clear colour */
+#define PBF_SSF_RGBA8 5         /* uint8 [h][w][4], PBF_SSF_COLOR quantised as an 8-bit framebuffer */
+
+typedef struct pbf_ssf_params {
+    uint32_t width, height;     /* 1280 x 720 (main.cpp:32) */
+    float projection[16];       /* column-major, the Scene block's Projection */
+    float view[16];             /* column-major, the Scene block's View (World = identity) */
+    float point_radius;         /* 0.18 (main.cpp:388) */
+    float point_scale;          /* sprite mode only: pixels per unit of point_radius / dist */
+    float near_plane, far_plane;/* 0.1, 50 (src/common/controls.cpp:25-26) */
+    float blur_radius;          /* 5.5e-6 (main.cpp:189) */
+    float blur_scale;           /* height / tanf(45 * 0.5 * 3.1415 / 180) (main.cpp:445) */
+    uint32_t blur_passes;       /* 3 (main.cpp:430-509) */
+    uint32_t splat_mode;        /* PBF_SSF_SPLAT_* */
+    float thickness;            /* thickness map value (see pbf_ssf_params_init) */
+    float clear_color[4];       /* 0.6, 0.6, 0.6, 1 (main.cpp:76) */
+} pbf_ssf_params;
+
+typedef struct pbf_ssf_renderer pbf_ssf_renderer;
+
+/* Defaults of the reference's first frame: controls.cpp's initial camera
+ * (position (2, 4, 10), angles pi and -0.1 pi, glm::perspective(45.0f,
+ * 4/3, 0.1, 50) with 45 taken as radians by GLM 0.9.7, glm::lookAt), all in
+ * float on the host.  The reference's thickness pass loads a fragment
+ * shader absent from its assets, so its thickness map is undefined; the
+ * default here is 0.6, the value its clear leaves in the map.  point_scale
+ * defaults to the projection's pixels per unit at unit distance. */
+pbf_status pbf_ssf_params_init(pbf_ssf_params *p);
+/* The projection must keep x on (x, z), y on (y, z), and clip z, w on (z, w)
+ * (any glm::perspective / frustum / ortho), else PBF_ERROR_BAD_PARAMETER.
+ * width and height: 1 .. 8192. */
+pbf_status pbf_ssf_create(int device, const pbf_ssf_params *p, pbf_ssf_renderer **out);
+pbf_status pbf_ssf_destroy(pbf_ssf_renderer *r);
+/* One frame from n positions (device, AoS float3, as the reference's VBO). */
+pbf_status pbf_ssf_render(pbf_ssf_renderer *r, const float *x_dev, uint32_t n, void *stream);
+/* One frame from a handle's / a batch scene's resident particles; the live
+ * count is read on the device (no host synchronisation). */
+pbf_status pbf_ssf_render_particles(pbf_ssf_renderer *r, pbf_handle *h, void *stream);
+pbf_status pbf_ssf_render_scene(pbf_ssf_renderer *r, pbf_batch *b, uint32_t scene_id, void *stream);
+/* Copy one image (PBF_SSF_*) out; blocks on the stream when dst is host. */
+pbf_status pbf_ssf_get_image(pbf_ssf_renderer *r, int which, void *dst, int dst_is_device, void *stream);
+/* Device address and size in bytes of one image buffer (valid until destroy). */
+pbf_status pbf_ssf_image_device(pbf_ssf_renderer *r, int which, void **ptr, uint64_t *bytes);
+/* The inverse projection and the normalised light direction the passes use. */
+pbf_status pbf_ssf_frame_constants(const pbf_ssf_renderer *r, float inv_projection[16], float incident[3]);
+/* Kernels launched by the last frame. */
+pbf_status pbf_ssf_last_launches(const pbf_ssf_renderer *r, uint32_t *n);
+
 /* ---- continuous-batching server ---- */
 typedef struct pbf_server_config {
     uint64_t hbm_budget_bytes;  /* admission budget for resident scenes */

@@ -16,7 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpbf_oracle.so")
-SOURCES = [os.path.join(HERE, "pbf_oracle.c")]
+SOURCES = [os.path.join(HERE, "pbf_oracle.c"), os.path.join(HERE, "ssf_oracle.c")]
 DEPS = SOURCES + [os.path.join(HERE, "pbf_oracle.h"), os.path.join(HERE, "pbf_oracle_solve.inc")]
 
 

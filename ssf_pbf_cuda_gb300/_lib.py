@@ -30,6 +30,8 @@ PBF_ARRANGE_VOLUME, PBF_ARRANGE_RECTANGLE, PBF_ARRANGE_LINE, PBF_ARRANGE_CYLINDE
 PBF_TENSILE_REFERENCE, PBF_TENSILE_TEXTBOOK, PBF_TENSILE_OFF = 0, 1, 2
 PBF_VORTICITY_OFF, PBF_VORTICITY_REFERENCE, PBF_VORTICITY_TEXTBOOK = 0, 1, 2
 PBF_XSPH_OFF, PBF_XSPH_WALK, PBF_XSPH_LIST = 0, 1, 2
+PBF_SSF_SPLAT_QUAD, PBF_SSF_SPLAT_SPRITE = 0, 1
+PBF_SSF_DEPTH, PBF_SSF_BLURRED, PBF_SSF_BLUR_INPUT, PBF_SSF_NORMAL, PBF_SSF_COLOR, PBF_SSF_RGBA8 = range(6)
 
 
 class PbfParams(ctypes.Structure):
@@ -47,6 +49,15 @@ class PbfArrangement(ctypes.Structure):
     _fields_ = [
         ("kind", c_i32), ("axis", c_i32), ("origin", c_f * 3), ("end", c_f * 3), ("axis_value", c_f),
         ("radius", c_f), ("height", c_f), ("space", c_f),
+    ]
+
+
+class PbfSsfParams(ctypes.Structure):
+    _fields_ = [
+        ("width", c_u32), ("height", c_u32), ("projection", c_f * 16), ("view", c_f * 16),
+        ("point_radius", c_f), ("point_scale", c_f), ("near_plane", c_f), ("far_plane", c_f),
+        ("blur_radius", c_f), ("blur_scale", c_f), ("blur_passes", c_u32), ("splat_mode", c_u32),
+        ("thickness", c_f), ("clear_color", c_f * 4),
     ]
 
 
@@ -142,6 +153,16 @@ SIGNATURES = {
     "pbf_batch_get_particles_by_id": (c_i32, [c_vp, c_u32, c_vp, c_vp, c_u32, ctypes.c_int, c_vp]),
     "pbf_batch_generate": (c_i32, [c_vp, c_u32, P(PbfArrangement), P(c_f), c_vp, P(c_u32)]),
     "pbf_batch_emit": (c_i32, [c_vp, c_u32, c_vp, ctypes.c_double, c_vp]),
+    "pbf_ssf_params_init": (c_i32, [P(PbfSsfParams)]),
+    "pbf_ssf_create": (c_i32, [ctypes.c_int, P(PbfSsfParams), P(c_vp)]),
+    "pbf_ssf_destroy": (c_i32, [c_vp]),
+    "pbf_ssf_render": (c_i32, [c_vp, c_vp, c_u32, c_vp]),
+    "pbf_ssf_render_particles": (c_i32, [c_vp, c_vp, c_vp]),
+    "pbf_ssf_render_scene": (c_i32, [c_vp, c_vp, c_u32, c_vp]),
+    "pbf_ssf_get_image": (c_i32, [c_vp, ctypes.c_int, c_vp, ctypes.c_int, c_vp]),
+    "pbf_ssf_image_device": (c_i32, [c_vp, ctypes.c_int, P(c_vp), P(c_u64)]),
+    "pbf_ssf_frame_constants": (c_i32, [c_vp, P(c_f), P(c_f)]),
+    "pbf_ssf_last_launches": (c_i32, [c_vp, P(c_u32)]),
     "pbf_server_create": (c_i32, [P(PbfServerConfig), P(c_vp)]),
     "pbf_server_destroy": (c_i32, [c_vp]),
     "pbf_server_submit": (c_i32, [c_vp, P(PbfRequestDesc), c_vp, c_vp, c_u32, P(c_u64)]),

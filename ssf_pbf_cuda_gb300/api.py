@@ -657,3 +657,119 @@ class Server:
 
     def clock(self) -> float:
         return load().pbf_server_clock(self.handle)
+
+
+# ------------------------------------------------------------- rendering --
+
+# image name -> (PBF_SSF_* id, dtype, channels)
+SSF_IMAGES = {
+    "depth": (L.PBF_SSF_DEPTH, np.float32, 1),
+    "blurred": (L.PBF_SSF_BLURRED, np.float32, 1),
+    "blur_input": (L.PBF_SSF_BLUR_INPUT, np.float32, 1),
+    "normal": (L.PBF_SSF_NORMAL, np.float32, 4),
+    "color": (L.PBF_SSF_COLOR, np.float32, 4),
+    "rgba8": (L.PBF_SSF_RGBA8, np.uint8, 4),
+}
+_SSF_ARRAYS = {"projection": 16, "view": 16, "clear_color": 4}
+
+
+def ssf_default_params(**overrides) -> dict:
+    """The reference's first rendered frame: 1280 x 720 (src/main.cpp:32),
+    the camera of src/common/controls.cpp:12-110, point radius 0.18
+    (main.cpp:388), blur radius 5.5e-6 and three blur passes
+    (main.cpp:189, 430-509); see ``pbf_ssf_params_init``."""
+    s = L.PbfSsfParams()
+    check(load().pbf_ssf_params_init(ctypes.byref(s)), "pbf_ssf_params_init")
+    d = {}
+    for k, _ in L.PbfSsfParams._fields_:
+        v = getattr(s, k)
+        d[k] = np.array(v[:], np.float32) if k in _SSF_ARRAYS else v
+    for k, v in overrides.items():
+        if k not in d:
+            raise KeyError(k)
+        d[k] = v
+    return d
+
+
+def _ssf_struct(d: dict) -> L.PbfSsfParams:
+    s = L.PbfSsfParams()
+    for k, _ in L.PbfSsfParams._fields_:
+        v = d[k]
+        if k in _SSF_ARRAYS:
+            a = np.asarray(v, np.float32).reshape(-1)
+            getattr(s, k)[:] = [float(t) for t in a]
+        else:
+            setattr(s, k, v)
+    return s
+
+
+class SsfRenderer:
+    """Headless screen-space fluid renderer: the reference's per-frame GL
+    passes (src/main.cpp:372-564) as CUDA kernels into device images.
+    Images come back as numpy arrays with row 0 at the bottom."""
+
+    def __init__(self, params: dict | None = None, device: int = 0, **overrides):
+        self.params = dict(params) if params is not None else ssf_default_params()
+        self.params.update(overrides)
+        h = ctypes.c_void_p()
+        check(load().pbf_ssf_create(device, ctypes.byref(_ssf_struct(self.params)), ctypes.byref(h)),
+              "pbf_ssf_create")
+        self.handle = h.value
+        self.device = device
+        self.width, self.height = int(self.params["width"]), int(self.params["height"])
+
+    def __del__(self):
+        h, self.handle = getattr(self, "handle", None), None
+        if h:
+            try:
+                load().pbf_ssf_destroy(h)
+            except Exception:
+                pass
+
+    def render(self, x, stream=None):
+        """One frame of n positions: a torch CUDA tensor (n, 3) float32, or a
+        host array (copied to the device first)."""
+        if not _is_device(x):
+            import torch
+            x = torch.from_numpy(_host3(x)).to(f"cuda:{self.device}")
+        x = x.contiguous()
+        check(load().pbf_ssf_render(self.handle, x.data_ptr(), x.shape[0], _stream(stream)), "pbf_ssf_render")
+        self._keep = x  # the frame reads x until the stream reaches its end
+
+    def render_particles(self, part: "PbfParticle", stream=None):
+        check(load().pbf_ssf_render_particles(self.handle, part.handle, _stream(stream)), "pbf_ssf_render_particles")
+
+    def render_scene(self, batch: "Batch", sid: int, stream=None):
+        check(load().pbf_ssf_render_scene(self.handle, batch.handle, sid, _stream(stream)), "pbf_ssf_render_scene")
+
+    def image(self, which: str = "rgba8", stream=None) -> np.ndarray:
+        kind, dt, ch = SSF_IMAGES[which]
+        shape = (self.height, self.width) if ch == 1 else (self.height, self.width, ch)
+        out = np.zeros(shape, dt)
+        check(load().pbf_ssf_get_image(self.handle, kind, out.ctypes.data, 0, _stream(stream)), "pbf_ssf_get_image")
+        return out
+
+    def image_device(self, which: str) -> tuple:
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_uint64()
+        check(load().pbf_ssf_image_device(self.handle, SSF_IMAGES[which][0], ctypes.byref(ptr), ctypes.byref(nbytes)),
+              "pbf_ssf_image_device")
+        return ptr.value, nbytes.value
+
+    def frame_constants(self) -> tuple:
+        inv = (ctypes.c_float * 16)()
+        inc = (ctypes.c_float * 3)()
+        check(load().pbf_ssf_frame_constants(self.handle, inv, inc), "pbf_ssf_frame_constants")
+        return np.array(inv[:], np.float32), np.array(inc[:], np.float32)
+
+    @property
+    def launches(self) -> int:
+        n = ctypes.c_uint32()
+        check(load().pbf_ssf_last_launches(self.handle, ctypes.byref(n)), "pbf_ssf_last_launches")
+        return n.value
+
+    def save_ppm(self, path: str, stream=None):
+        """The composited frame as a binary PPM (top row first)."""
+        img = self.image("rgba8", stream)[::-1, :, :3]
+        with open(path, "wb") as fh:
+            fh.write(f"P6\n{self.width} {self.height}\n255\n".encode())
+            fh.write(np.ascontiguousarray(img).tobytes())

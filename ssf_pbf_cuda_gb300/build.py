@@ -19,7 +19,11 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpbf103.so")
 
-SOURCES = ["pbf_kernels.cu", "pbf_engine.cu", "pbf_capi.cu", "pbf_server.cu", "pbf_noalloc.cu", "pbf_particles.cu"]
+SOURCES = ["pbf_kernels.cu", "pbf_engine.cu", "pbf_capi.cu", "pbf_server.cu", "pbf_noalloc.cu", "pbf_particles.cu",
+           "pbf_ssf.cu"]
+# per-file flags: the screen-space passes round every product and sum on its
+# own (no contraction into FMA), as their CPU restatement does
+FILE_FLAGS = {"pbf_ssf.cu": ["-fmad=false"]}
 HEADERS = ["pbf_internal.h", "pbf_engine.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,7 +59,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s, *hdrs, __file__]):
-            cmd = [nvcc(), *_flags(extra_flags), "-c", s, "-o", o]
+            cmd = [nvcc(), *_flags(extra_flags), *FILE_FLAGS.get(src, []), "-c", s, "-o", o]
             if verbose and src == "pbf_kernels.cu":
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
