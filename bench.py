@@ -402,6 +402,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ssf", action="store_true", help="skip the screen-space fluid frame timing")
+    ap.add_argument("--ssf-only", action="store_true",
+                    help="time only the screen-space fluid frames and print their JSON object")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
     ap.add_argument("--preheat", type=float, default=3.0,
                     help="seconds of untimed steps before the warm-up: a GPU coming out of idle runs the first "
@@ -430,6 +432,11 @@ def main():
 
     from ssf_pbf_cuda_gb300 import api, build
     build.build()
+
+    if args.ssf_only:
+        if rank == 0:
+            print(json.dumps({"ssf_frame": run_ssf_bench(api, torch, local, not args.no_cpu)}), flush=True)
+        return
 
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)

@@ -12,7 +12,8 @@
  *   shading       asset/shader/ssf_shading.frag:23-83, blended onto the
  *                 clear colour (main.cpp:76, 541-564).
  * Fixed-function steps are written as the GL specification states them:
- * viewport transform, pixel-centre coverage, point-sprite coordinates with
+ * viewport transform, pixel-centre coverage (tex_coord of pixel i taken as
+ * (i + 0.5) * (1 / width)), point-sprite coordinates with
  * the upper-left origin, LINEAR + CLAMP_TO_EDGE filtering (weights with 8
  * fractional bits, as a texture unit keeps them), gl_FragDepth clamped to
  * [0, 1] and tested GL_LESS against the cleared 1.0, fine 2x2-quad
@@ -66,6 +67,7 @@ static int maxi(int a, int b) { return a > b ? a : b; }
  * of one particle share; 0 = nothing of it reaches the image. */
 typedef struct {
     float x0, x1, y0, y1, ax, ay, dx, by, ex, ey, ez;
+    float rx, ry; /* 1 / window width, height of the quad; sprite: 1 / size */
     int i0, j0, i1, j1;
 } Footprint;
 
@@ -94,6 +96,8 @@ static int footprint(const OraSsf *f, float px, float py, float pz, Footprint *s
         s->y0 = ca.y / ca.w * hh + hh;
         s->y1 = cb.y / cb.w * hh + hh;
         if (!(s->x1 > s->x0 && s->y1 > s->y0)) return 0; /* back face culled */
+        s->rx = 1.f / (s->x1 - s->x0);
+        s->ry = 1.f / (s->y1 - s->y0);
     } else {
         /* ssf_point_sprite.vert:20-26 */
         float dist = sqrtf(dot3(e.x, e.y, e.z, e.x, e.y, e.z));
@@ -110,6 +114,7 @@ static int footprint(const OraSsf *f, float px, float py, float pz, Footprint *s
         s->ay = yw;
         s->dx = size;
         s->by = 0.f;
+        s->rx = s->ry = 1.f / size;
     }
     s->i0 = maxi(clamp_pix(floorf(s->x0 - 0.5f), f->w), 0);
     s->j0 = maxi(clamp_pix(floorf(s->y0 - 0.5f), f->h), 0);
@@ -125,13 +130,15 @@ static float fragment(const OraSsf *f, const Footprint *s, int i, int j)
     if (!(cx >= s->x0 && cx < s->x1 && cy >= s->y0 && cy < s->y1)) return -1.f;
     float nx, ny, px, py, pz;
     if (f->mode == 0) {
-        float u = (cx - s->x0) / (s->x1 - s->x0), v = (cy - s->y0) / (s->y1 - s->y0);
+        /* vertex_uv: screen-space interpolation over the quad (w is constant
+         * on it), as (c - corner) * (1 / extent) */
+        float u = (cx - s->x0) * s->rx, v = (cy - s->y0) * s->ry;
         nx = u * 2.f - 1.f; /* vertex_uv * 2 - 1 */
         ny = v * 2.f - 1.f;
         px = s->ax + u * (s->dx - s->ax); /* pos_from_eye, interpolated */
         py = s->ay + v * (s->by - s->ay);
     } else {
-        float sc = 0.5f + (cx - s->ax) / s->dx, tc = 0.5f - (cy - s->ay) / s->dx; /* gl_PointCoord */
+        float sc = 0.5f + (cx - s->ax) * s->rx, tc = 0.5f - (cy - s->ay) * s->ry; /* gl_PointCoord */
         nx = sc * 2.f + -1.f;
         ny = tc * -2.f + 1.f;
         px = s->ex;
@@ -147,7 +154,7 @@ static float fragment(const OraSsf *f, const Footprint *s, int i, int j)
     float cw = f->proj[3] * px + f->proj[7] * py + f->proj[11] * pz + f->proj[15];
     float d = cz / cw;
     if (d != d) return -1.f;
-    return fminf(fmaxf(d, 0.f), 1.f);
+    return fminf(fmaxf(d, 0.f), 1.f) + 0.f; /* clamped to the depth range, -0 as +0 */
 }
 
 /* depth[h][w]: cleared to 1, then the nearest fragment of every particle.
@@ -212,7 +219,7 @@ void ora_ssf_blur(const OraSsf *f, const float *in, float *out)
 {
     for (uint32_t j = 0; j < f->h; ++j)
         for (uint32_t i = 0; i < f->w; ++i) {
-            float s = ((float)i + 0.5f) / (float)f->w, t = ((float)j + 0.5f) / (float)f->h;
+            float s = ((float)i + 0.5f) * (1.f / (float)f->w), t = ((float)j + 0.5f) * (1.f / (float)f->h);
             float ed = sample(in, f->w, f->h, s, t);
             if (ed == 1.f) {
                 out[(size_t)j * f->w + i] = 1.f;
@@ -247,7 +254,7 @@ void ora_ssf_blur(const OraSsf *f, const float *in, float *out)
 static void eye_at(const OraSsf *f, const float *D, int i, int j, float out[3])
 {
     int ic = mini(maxi(i, 0), (int)f->w - 1), jc = mini(maxi(j, 0), (int)f->h - 1);
-    float s = ((float)i + 0.5f) / (float)f->w, t = ((float)j + 0.5f) / (float)f->h;
+    float s = ((float)i + 0.5f) * (1.f / (float)f->w), t = ((float)j + 0.5f) * (1.f / (float)f->h);
     uv_to_eye(f, s, t, D[(size_t)jc * f->w + ic], 0, out);
 }
 
@@ -294,7 +301,7 @@ void ora_ssf_shade(const OraSsf *f, const float *D, const float *N, float *C, ui
             } else {
                 const float *n = N + 4 * o;
                 float th = clamp01(f->thickness);
-                float s = ((float)i + 0.5f) / (float)f->w, t = ((float)j + 0.5f) / (float)f->h;
+                float s = ((float)i + 0.5f) * (1.f / (float)f->w), t = ((float)j + 0.5f) * (1.f / (float)f->h);
                 float p[3];
                 uv_to_eye(f, s, t, ed, 1, p);
                 float il = f->incident[0], jl = f->incident[1], kl = f->incident[2];

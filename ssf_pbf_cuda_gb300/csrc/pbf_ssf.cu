@@ -43,6 +43,7 @@ struct Frame {
     float blur_radius, blur_scale, thickness, pad1;
     float clear[4];
     float incident[3];
+    float inv_w, inv_h;  // 1 / width, 1 / height: tex_coord = (i + 0.5) * inv_w
 };
 
 // GLSL mat4 * vec4 (column-major), summed in column order.
@@ -59,13 +60,13 @@ __host__ __device__ inline float dot3(float ax, float ay, float az, float bx, fl
 
 // ------------------------------------------------------------ depth splat --
 
-// Everything the fragments of one particle share.
+// What the fragments of one particle share.
 struct Splat {
-    float x0, x1, y0, y1;      // covered pixel centres: x0 <= cx < x1, y0 <= cy < y1 (window)
-    float ax, ay, dx, by;      // quad: view-space corner a (left-bottom), d.x, b.y
-    float ex, ey, ez;          // view-space centre (pos_from_eye of a sprite)
-    int i0, j0;                // candidate pixel box
-    uint32_t bw, bh;
+    float x0, y0;       // quad: window corner a; sprite: window centre
+    float rx, ry;       // quad: 1 / window width, height of the quad; sprite: 1 / size
+    float ez;           // view-space depth of the centre (pos_from_eye.z)
+    int i0, j0;         // first covered pixel column / row
+    uint32_t bw, bh;    // covered pixel box
 };
 
 __device__ inline int clamp_pix(float v, uint32_t n)
@@ -74,33 +75,46 @@ __device__ inline int clamp_pix(float v, uint32_t n)
     return (int)v;
 }
 
+// Pixels whose centre c satisfies lo <= c < hi: [first, last], clipped to
+// the image; false when none.
+__device__ inline bool centre_range(float lo, float hi, uint32_t n, int &first, int &last)
+{
+    int a = max(clamp_pix(floorf(lo - 0.5f), n), 0);
+    for (int k = 0; k < 3 && a < (int)n && !((float)a + 0.5f >= lo); ++k) ++a;
+    int b = min(clamp_pix(floorf(hi - 0.5f) + 1.f, n), (int)n - 1);
+    for (int k = 0; k < 3 && b >= a && !((float)b + 0.5f < hi); ++k) --b;
+    first = a;
+    last = b;
+    return a <= b && a < (int)n && (float)a + 0.5f >= lo && (float)b + 0.5f < hi;
+}
+
 // Per-particle set-up.  false: nothing of the particle reaches the image.
 __device__ inline bool splat_setup(const Frame &f, float px, float py, float pz, Splat &s)
 {
     const float4 e = mat_vec(f.view, px, py, pz, 1.f);  // vw * vec4(Position, 1), World = identity
     const float hw = (float)f.w * 0.5f, hh = (float)f.h * 0.5f;
-    s.ex = e.x;
-    s.ey = e.y;
     s.ez = e.z;
+    float x0, x1, y0, y1;
     if (f.mode == PBF_SSF_SPLAT_QUAD) {
         // ssf_object.geom:21-50: corners P.xy +- 0.5 point_radius at P.zw
         const float hr = 0.5f * f.radius;
-        s.ax = e.x - hr;
-        s.ay = e.y - hr;
-        s.dx = e.x + hr;
-        s.by = e.y + hr;
-        const float4 ca = mat_vec(f.proj, s.ax, s.ay, e.z, e.w);
-        const float4 cd = mat_vec(f.proj, s.dx, s.ay, e.z, e.w);
-        const float4 cb = mat_vec(f.proj, s.ax, s.by, e.z, e.w);
+        const float ax = e.x - hr, ay = e.y - hr, dx = e.x + hr, by = e.y + hr;
+        const float4 ca = mat_vec(f.proj, ax, ay, e.z, e.w);
+        const float4 cd = mat_vec(f.proj, dx, ay, e.z, e.w);
+        const float4 cb = mat_vec(f.proj, ax, by, e.z, e.w);
         // clip z and w depend on (z, w) alone, so the four corners clip alike
         if (!(-ca.w <= ca.z && ca.z <= ca.w)) return false;
-        s.x0 = ca.x / ca.w * hw + hw;
-        s.x1 = cd.x / cd.w * hw + hw;
-        s.y0 = ca.y / ca.w * hh + hh;
-        s.y1 = cb.y / cb.w * hh + hh;
+        x0 = ca.x / ca.w * hw + hw;
+        x1 = cd.x / cd.w * hw + hw;
+        y0 = ca.y / ca.w * hh + hh;
+        y1 = cb.y / cb.w * hh + hh;
         // counter-clockwise strip a, d, b, c is front-facing; a mirrored
         // quad is culled (GL_CULL_FACE, main.cpp:73)
-        if (!(s.x1 > s.x0 && s.y1 > s.y0)) return false;
+        if (!(x1 > x0 && y1 > y0)) return false;
+        s.x0 = x0;
+        s.y0 = y0;
+        s.rx = 1.f / (x1 - x0);
+        s.ry = 1.f / (y1 - y0);
     } else {
         // ssf_point_sprite.vert:19-27: size = pointRadius * (pointScale / dist)
         const float dist = sqrtf(dot3(e.x, e.y, e.z, e.x, e.y, e.z));
@@ -110,84 +124,154 @@ __device__ inline bool splat_setup(const Frame &f, float px, float py, float pz,
         if (!(-c.w <= c.x && c.x <= c.w && -c.w <= c.y && c.y <= c.w && -c.w <= c.z && c.z <= c.w)) return false;
         if (!(size > 0.f)) return false;
         const float xw = c.x / c.w * hw + hw, yw = c.y / c.w * hh + hh, half = size * 0.5f;
-        s.x0 = xw - half;
-        s.x1 = xw + half;
-        s.y0 = yw - half;
-        s.y1 = yw + half;
-        s.ax = xw;    // sprite: window centre and size ride in ax / ay / dx
-        s.ay = yw;
-        s.dx = size;
-        s.by = 0.f;
+        x0 = xw - half;
+        x1 = xw + half;
+        y0 = yw - half;
+        y1 = yw + half;
+        s.x0 = xw;
+        s.y0 = yw;
+        s.rx = s.ry = 1.f / size;
     }
-    const int i0 = clamp_pix(floorf(s.x0 - 0.5f), f.w), i1 = clamp_pix(floorf(s.x1 - 0.5f) + 1.f, f.w);
-    const int j0 = clamp_pix(floorf(s.y0 - 0.5f), f.h), j1 = clamp_pix(floorf(s.y1 - 0.5f) + 1.f, f.h);
-    s.i0 = max(i0, 0);
-    s.j0 = max(j0, 0);
-    const int ie = min(i1, (int)f.w - 1), je = min(j1, (int)f.h - 1);
-    if (ie < s.i0 || je < s.j0) return false;
-    s.bw = (uint32_t)(ie - s.i0 + 1);
-    s.bh = (uint32_t)(je - s.j0 + 1);
+    int i1, j1;
+    if (!centre_range(x0, x1, f.w, s.i0, i1) || !centre_range(y0, y1, f.h, s.j0, j1)) return false;
+    s.bw = (uint32_t)(i1 - s.i0 + 1);
+    s.bh = (uint32_t)(j1 - s.j0 + 1);
     return true;
 }
 
 // One fragment: ssf_object.frag:18-35 / ssf_point_sprite.frag:17-31.
 // Returns the window depth, or a negative value when nothing is written.
+// With the projection's z and w rows free of x and y, the depth needs only
+// the z of pixelPos: clip.z / clip.w = (P22 z + P32) / (P23 z + P33).
 __device__ inline float splat_fragment(const Frame &f, const Splat &s, int i, int j)
 {
     const float cx = (float)i + 0.5f, cy = (float)j + 0.5f;
-    if (!(cx >= s.x0 && cx < s.x1 && cy >= s.y0 && cy < s.y1)) return -1.f;
-    float nx, ny, px, py, pz;
+    float nx, ny;
     if (f.mode == PBF_SSF_SPLAT_QUAD) {
-        // vertex_uv over the quad; w is constant on it, so the perspective-
+        // vertex_uv * 2 - 1; w is constant over the quad, so the perspective-
         // correct interpolation is the screen-space one
-        const float u = (cx - s.x0) / (s.x1 - s.x0), v = (cy - s.y0) / (s.y1 - s.y0);
-        nx = u * 2.f - 1.f;
-        ny = v * 2.f - 1.f;
-        px = s.ax + u * (s.dx - s.ax);  // pos_from_eye
-        py = s.ay + v * (s.by - s.ay);
+        nx = ((cx - s.x0) * s.rx) * 2.f - 1.f;
+        ny = ((cy - s.y0) * s.ry) * 2.f - 1.f;
     } else {
-        // gl_PointCoord, origin upper left
-        const float sc = 0.5f + (cx - s.ax) / s.dx, tc = 0.5f - (cy - s.ay) / s.dx;
-        nx = sc * 2.f + -1.f;
-        ny = tc * -2.f + 1.f;
-        px = s.ex;
-        py = s.ey;
+        // gl_PointCoord (origin upper left) * (2, -2) + (-1, 1)
+        nx = (0.5f + (cx - s.x0) * s.rx) * 2.f + -1.f;
+        ny = (0.5f - (cy - s.y0) * s.ry) * -2.f + 1.f;
     }
     const float mag = nx * nx + ny * ny;
     if (mag > 1.f) return -1.f;  // discard: outside the circle
-    const float nz = sqrtf(1.f - mag);
-    px = px + nx * f.radius;
-    py = py + ny * f.radius;
-    pz = s.ez + nz * f.radius;
-    const float cz = f.proj[2] * px + f.proj[6] * py + f.proj[10] * pz + f.proj[14];
-    const float cw = f.proj[3] * px + f.proj[7] * py + f.proj[11] * pz + f.proj[15];
-    const float d = cz / cw;  // gl_FragDepth = clip.z / clip.w
+    const float pz = s.ez + sqrtf(1.f - mag) * f.radius;
+    const float d = (f.proj[10] * pz + f.proj[14]) / (f.proj[11] * pz + f.proj[15]);
     if (d != d) return -1.f;
-    return fminf(fmaxf(d, 0.f), 1.f);  // clamped to the depth range
+    return fminf(fmaxf(d, 0.f), 1.f) + 0.f;  // clamped to the depth range; + 0 turns -0 into +0
 }
 
-// One warp per particle, lanes over the particle's pixel box; the depth test
-// (GL_LESS against the cleared 1.0) is an atomic minimum on the float bits,
-// which order like the values for depths in [0, 1].
+// Early depth rejection, exact: no fragment of the particle is nearer than
+// its front point (nz = 1) by more than the rounding of the depth formula,
+// so a pixel already holding a depth at or below the bound keeps it.
+__device__ inline uint32_t front_bound(const Frame &f, float ez)
+{
+    const float pz = ez + f.radius;
+    const float num = f.proj[10] * pz + f.proj[14], den = f.proj[11] * pz + f.proj[15];
+    const float d = num / den;
+    // |float - exact| <= 2^-22 (|P22 pz| + |P32|) / |den| + ulp / 2; four times that
+    const float err = 4.f * (2.3841858e-7f * (fabsf(f.proj[10] * pz) + fabsf(f.proj[14])) / fabsf(den) + 6e-8f);
+    const float b = d - err;
+    if (!(b > 0.f)) return 0u;  // also NaN
+    return __float_as_uint(fminf(b, 1.f));
+}
+
+// A particle's splat as the raster kernel reads it (32 B): (x0, y0, rx, ry)
+// and (ez bits, depth bound bits, i0 | j0 << 16, bw | bh << 16); bw = 0 when
+// nothing of the particle reaches the image.
+struct SplatRec {
+    float4 a;
+    uint4 b;
+};
+
+// One thread per particle: the per-particle set-up, once.
 template <int STRIDE>
-__global__ void __launch_bounds__(256) k_ssf_splat(const float *__restrict__ x, const uint32_t *__restrict__ n_dev,
-                                                   uint32_t n_arg, Frame f, uint32_t *__restrict__ depth)
+__global__ void __launch_bounds__(256) k_ssf_setup(const float *__restrict__ x, const uint32_t *__restrict__ n_dev,
+                                                   uint32_t n_arg, Frame f, SplatRec *__restrict__ rec)
+{
+    const uint32_t n = n_dev ? *n_dev : n_arg;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const float *xp = x + (size_t)p * STRIDE;
+        Splat s;
+        SplatRec r;
+        if (splat_setup(f, __ldg(xp), __ldg(xp + 1), __ldg(xp + 2), s)) {
+            r.a = make_float4(s.x0, s.y0, s.rx, s.ry);
+            r.b = make_uint4(__float_as_uint(s.ez), front_bound(f, s.ez), (uint32_t)s.i0 | ((uint32_t)s.j0 << 16),
+                             s.bw | (s.bh << 16));
+        } else {
+            r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+            r.b = make_uint4(0u, 0u, 0u, 0u);
+        }
+        rec[p] = r;
+    }
+}
+
+// One warp per particle, lanes over its pixel box (stepped without
+// division).  The depth test (GL_LESS against the cleared 1.0) is an atomic
+// minimum on the float bits, which order like the values in [0, 1]; the
+// result does not depend on the order of fragments.
+__global__ void __launch_bounds__(256) k_ssf_raster(const SplatRec *__restrict__ rec,
+                                                    const uint32_t *__restrict__ n_dev, uint32_t n_arg, Frame f,
+                                                    uint32_t *__restrict__ depth)
 {
     const uint32_t n = n_dev ? *n_dev : n_arg;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += warps) {
-        const float *xp = x + (size_t)p * STRIDE;
-        Splat s;
-        if (!splat_setup(f, __ldg(xp), __ldg(xp + 1), __ldg(xp + 2), s)) continue;
-        const uint32_t npx = s.bw * s.bh;
-        for (uint32_t k = lane; k < npx; k += 32u) {
-            const int i = s.i0 + (int)(k % s.bw), j = s.j0 + (int)(k / s.bw);
-            const float d = splat_fragment(f, s, i, j);
-            if (d < 0.f) continue;
-            uint32_t *dst = depth + (size_t)j * f.w + (uint32_t)i;
-            const uint32_t bits = __float_as_uint(d);
-            if (*dst > bits) atomicMin(dst, bits);
+        const uint4 rb = rec[p].b;
+        const uint32_t bw = rb.w & 0xffffu;
+        if (bw == 0u) continue;
+        const float4 ra = rec[p].a;
+        Splat q;
+        q.x0 = ra.x;
+        q.y0 = ra.y;
+        q.rx = ra.z;
+        q.ry = ra.w;
+        q.ez = __uint_as_float(rb.x);
+        q.i0 = (int)(rb.z & 0xffffu);
+        q.j0 = (int)(rb.z >> 16);
+        q.bw = bw;
+        q.bh = rb.w >> 16;
+        const uint32_t bound = rb.y;
+        const uint32_t dj = 32u / q.bw, di = 32u % q.bw;
+        // two cursors, 32 fragments apart, so two depth loads are in flight
+        uint32_t ci = lane % q.bw, cj = lane / q.bw;
+        uint32_t ci2 = ci + di, cj2 = cj + dj;
+        if (ci2 >= q.bw) {
+            ci2 -= q.bw;
+            ++cj2;
+        }
+        while (cj < q.bh) {
+            const bool two = cj2 < q.bh;
+            const int i1 = q.i0 + (int)ci, j1 = q.j0 + (int)cj, i2 = q.i0 + (int)ci2, j2 = q.j0 + (int)cj2;
+            uint32_t *d1 = depth + (size_t)j1 * f.w + (uint32_t)i1;
+            uint32_t *d2 = two ? depth + (size_t)j2 * f.w + (uint32_t)i2 : d1;
+            const uint32_t c1 = *d1, c2 = *d2;
+            if (c1 > bound) {
+                const float d = splat_fragment(f, q, i1, j1);
+                if (d >= 0.f && __float_as_uint(d) < c1) atomicMin(d1, __float_as_uint(d));
+            }
+            if (two && c2 > bound) {
+                const float d = splat_fragment(f, q, i2, j2);
+                if (d >= 0.f && __float_as_uint(d) < c2) atomicMin(d2, __float_as_uint(d));
+            }
+            // both cursors advance 64 fragments
+            ci = ci2 + di;
+            cj = cj2 + dj;
+            if (ci >= q.bw) {
+                ci -= q.bw;
+                ++cj;
+            }
+            ci2 = ci + di;
+            cj2 = cj + dj;
+            if (ci2 >= q.bw) {
+                ci2 -= q.bw;
+                ++cj2;
+            }
         }
     }
 }
@@ -210,8 +294,10 @@ __device__ inline float sample(const float *__restrict__ T, uint32_t W, uint32_t
     const int iu = clamp_pix(fu, W), iv = clamp_pix(fv, H);
     const int i0 = min(max(iu, 0), (int)W - 1), i1 = min(max(iu + 1, 0), (int)W - 1);
     const int j0 = min(max(iv, 0), (int)H - 1), j1 = min(max(iv + 1, 0), (int)H - 1);
-    const float t00 = __ldg(T + (size_t)j0 * W + i0), t10 = __ldg(T + (size_t)j0 * W + i1);
-    const float t01 = __ldg(T + (size_t)j1 * W + i0), t11 = __ldg(T + (size_t)j1 * W + i1);
+    // a texel with weight 0 adds +0 to a sum of non-negative terms: not loaded
+    const float *r0 = T + (size_t)j0 * W, *r1 = T + (size_t)j1 * W;
+    const float t00 = __ldg(r0 + i0), t10 = a != 0.f ? __ldg(r0 + i1) : 0.f;
+    const float t01 = b != 0.f ? __ldg(r1 + i0) : 0.f, t11 = (a != 0.f && b != 0.f) ? __ldg(r1 + i1) : 0.f;
     const float a1 = 1.f - a, b1 = 1.f - b;
     return (a1 * b1) * t00 + (a * b1) * t10 + (a1 * b) * t01 + (a * b) * t11;
 }
@@ -241,21 +327,28 @@ __device__ inline float depth_store(float v)
 }
 
 // ssf_blur.frag:44-139: 8 taps along s and 8 along t (the centre twice),
-// spatial weight exp(-x^2 r) and the range term as written.
+// spatial weight exp(-x^2 r) and the range term as written.  exp(-x^2 r)
+// depends on |x| only, so its five values are computed once; the range
+// weight is exp(-0) = 1 where the shader's r2 is 0.
 __global__ void __launch_bounds__(256) k_ssf_blur(const float *__restrict__ in, float *__restrict__ out, Frame f)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= f.w || j >= f.h) return;
-    const float s = ((float)i + 0.5f) / (float)f.w, t = ((float)j + 0.5f) / (float)f.h;
-    const float ed = sample(in, f.w, f.h, s, t);
+    // the centre tap: at a texel centre the 8-bit filter weights round to 0
+    // and 1 (sides up to 8192), so the filtered value is the texel itself
+    const float ed = __ldg(in + (size_t)j * f.w + i);
     if (ed == 1.f) {
         out[(size_t)j * f.w + i] = 1.f;
         return;
     }
+    const float s = ((float)i + 0.5f) * f.inv_w, t = ((float)j + 0.5f) * f.inv_h;
     const float lin = linearize(ed, f);
     const float3 p = uv_to_eye(f, s, t, ed, true);
     const float dist = sqrtf(dot3(p.x, p.y, p.z, p.x, p.y, p.z));
     const float br = f.blur_radius * f.blur_scale / dist;
+    float wk[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) wk[k] = expf(-((float)(k * k) * br));
     float sum = 0.f, wsum = 0.f;
 #pragma unroll
     for (int axis = 0; axis < 2; ++axis) {
@@ -265,11 +358,10 @@ __global__ void __launch_bounds__(256) k_ssf_blur(const float *__restrict__ in, 
                                        : sample(in, f.w, f.h, s, t + (float)k * br);
             if (sd != 1.f) {
                 const float sl = linearize(sd, f);
-                const float r = (float)(k * k) * br;
-                const float w = expf(-r);
+                const float w = wk[k < 0 ? -k : k];
                 const float diff = sl - lin;
                 const float r2 = fabsf(diff) < 0.01f ? diff * 100.f : 0.f;
-                const float g = expf(-r2 * r2);
+                const float g = r2 != 0.f ? expf(-r2 * r2) : 1.f;
                 sum = sum + sl * w * g;
                 wsum = wsum + w * g;
             }
@@ -282,7 +374,7 @@ __global__ void __launch_bounds__(256) k_ssf_blur(const float *__restrict__ in, 
 __device__ inline float3 eye_at(const Frame &f, const float *__restrict__ D, int i, int j)
 {
     const int ic = min(max(i, 0), (int)f.w - 1), jc = min(max(j, 0), (int)f.h - 1);
-    const float s = ((float)i + 0.5f) / (float)f.w, t = ((float)j + 0.5f) / (float)f.h;
+    const float s = ((float)i + 0.5f) * f.inv_w, t = ((float)j + 0.5f) * f.inv_h;
     return uv_to_eye(f, s, t, __ldg(D + (size_t)jc * f.w + ic), false);
 }
 
@@ -326,7 +418,7 @@ __global__ void __launch_bounds__(256) k_ssf_shade(const float *__restrict__ D, 
     } else {
         const float4 n = N[o];
         const float th = clamp01(f.thickness);
-        const float s = ((float)i + 0.5f) / (float)f.w, t = ((float)j + 0.5f) / (float)f.h;
+        const float s = ((float)i + 0.5f) * f.inv_w, t = ((float)j + 0.5f) * f.inv_h;
         const float3 p = uv_to_eye(f, s, t, ed, true);
         const float il = f.incident[0], jl = f.incident[1], kl = f.incident[2];
         const float vr = 1.f / sqrtf(dot3(-p.x, -p.y, -p.z, -p.x, -p.y, -p.z));
@@ -396,6 +488,8 @@ struct pbf_ssf_renderer {
     float4 *normal = nullptr, *color = nullptr;
     uchar4 *rgba8 = nullptr;
     const float *blurred = nullptr, *blur_input = nullptr;
+    SplatRec *rec = nullptr;   // per-particle splat records, grown to the largest particle bound seen
+    uint32_t rec_cap = 0;
     uint32_t launches = 0;
 };
 
@@ -429,12 +523,23 @@ pbf_status launch_frame(pbf_ssf_renderer *r, const float *x, int stride, const u
     k_ssf_fill<<<std::min<uint32_t>((px + 255) / 256, (uint32_t)r->sms * 8), 256, 0, st>>>(r->depth, kEmptyDepth, px);
     ++launches;
     if (n_upper) {
-        const uint32_t blocks = std::min<uint32_t>((n_upper + 7) / 8, (uint32_t)r->sms * 8);
+        if (n_upper > r->rec_cap) {
+            // the only allocation on the frame path: the first frame of a
+            // larger particle bound (cudaFree waits for frames in flight)
+            CK(cudaFree(r->rec));
+            r->rec = nullptr;
+            r->rec_cap = 0;
+            CK(cudaMalloc(&r->rec, sizeof(SplatRec) * (size_t)n_upper));
+            r->rec_cap = n_upper;
+        }
+        const uint32_t sblocks = std::min<uint32_t>((n_upper + 255) / 256, (uint32_t)r->sms * 8);
         if (stride == 4)
-            k_ssf_splat<4><<<blocks, 256, 0, st>>>(x, n_dev, n, f, r->depth);
+            k_ssf_setup<4><<<sblocks, 256, 0, st>>>(x, n_dev, n, f, r->rec);
         else
-            k_ssf_splat<3><<<blocks, 256, 0, st>>>(x, n_dev, n, f, r->depth);
-        ++launches;
+            k_ssf_setup<3><<<sblocks, 256, 0, st>>>(x, n_dev, n, f, r->rec);
+        const uint32_t rblocks = std::min<uint32_t>((n_upper + 7) / 8, (uint32_t)r->sms * 8);
+        k_ssf_raster<<<rblocks, 256, 0, st>>>(r->rec, n_dev, n, f, r->depth);
+        launches += 2;
     }
     const dim3 blk(32, 8), grd((f.w + 31) / 32, (f.h + 7) / 8);
     const float *src = reinterpret_cast<const float *>(r->depth), *prev = src;
@@ -479,6 +584,7 @@ void free_renderer(pbf_ssf_renderer *r)
     cudaFree(r->normal);
     cudaFree(r->color);
     cudaFree(r->rgba8);
+    cudaFree(r->rec);
     delete r;
 }
 
@@ -588,6 +694,8 @@ pbf_status pbf_ssf_create(int device, const pbf_ssf_params *p, pbf_ssf_renderer 
     f.blur_scale = p->blur_scale;
     f.thickness = p->thickness;
     std::memcpy(f.clear, p->clear_color, sizeof f.clear);
+    f.inv_w = 1.f / (float)f.w;
+    f.inv_h = 1.f / (float)f.h;
     // lightDir = View * World * vec4(1, 4, 1, 0) (ssf_shading.frag:39), normalised once
     const float4 l = mat_vec(f.view, 1.f, 4.f, 1.f, 0.f);
     float inc[3] = {l.x, l.y, l.z};

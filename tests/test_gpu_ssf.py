@@ -65,7 +65,7 @@ def test_dam_frame_pass_parity(gpu):
     r.render(torch.from_numpy(sc.x).to(gpu))
     g = _check_passes(r, sc.x, _frame(r))
     assert int((g["depth"] < 1).sum()) > 20000
-    assert r.launches == 7
+    assert r.launches == 8
 
 
 @pytest.mark.parametrize("mode", [api.L.PBF_SSF_SPLAT_QUAD, api.L.PBF_SSF_SPLAT_SPRITE])
@@ -101,7 +101,7 @@ def test_zero_blur_passes_and_empty_frame(gpu):
     r.render(x)
     g = _check_passes(r, x, _frame(r))
     assert np.array_equal(g["blurred"], g["depth"])
-    assert r.launches == 4
+    assert r.launches == 5
     r.render(np.zeros((0, 3), np.float32))
     g = _images(r)
     assert np.all(g["depth"] == 1)
