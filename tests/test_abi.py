@@ -81,6 +81,11 @@ STRUCTS = {
     "pbf_completion": ("PbfCompletion", ["request_id", "num", "flags", "arrival_s", "complete_s"]),
     "pbf_server_stats": ("PbfServerStats", ["submitted", "particle_steps", "resident_scenes", "busy_s",
                                             "elapsed_s"]),
+    "pbf_arrangement": ("PbfArrangement", ["kind", "axis", "origin", "end", "axis_value", "radius", "height",
+                                           "space"]),
+    "pbf_ssf_params": ("PbfSsfParams", ["width", "height", "projection", "view", "point_radius", "point_scale",
+                                        "near_plane", "far_plane", "blur_radius", "blur_scale", "blur_passes",
+                                        "splat_mode", "thickness", "clear_color"]),
 }
 
 
