@@ -177,7 +177,7 @@ Batch::~Batch()
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
                     d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
-                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_};
+                    d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_, d_mid_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -199,7 +199,8 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     max_cells_ = max_cells;
     max_pair_ = max_pair;
     bnd_capacity_ = (uint64_t)max_scenes * 32 + 1024;
-    max_tiles_ = max_particles / 64 + max_scenes + 1;
+    // particle tiles (64 particles at the smallest tile) then cell tiles
+    max_tiles_ = max_particles / 64 + max_scenes + 1 + max_cells / kCellTile + max_scenes + 1;
     const uint64_t P = max_particles, C = max_cells;
     auto A = [&](void **p, uint64_t bytes) -> cudaError_t {
         arena_bytes_ += bytes;
@@ -224,6 +225,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_nnb_, P));
     CK(A((void **)&d_cls_, P));
     CK(A((void **)&d_dense_, 4 * (2 * (P / 64 + 1) + 1)));  // a dense bucket holds more than 64 particles
+    CK(A((void **)&d_mid_, 4 * (2 * (P / 16 + 1) + 1)));    // a medium one more than 16
     CK(A((void **)&d_chist_, 8 * (C + 4)));
     CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
     CK(A((void **)&d_pack_off_, 4ull * max_scenes));
@@ -583,6 +585,16 @@ void Batch::rebuild_tiles()
         }
     }
     ctrl_.n_tiles = (uint32_t)tile_scene_.size();
+    // cell tiles: every cell of every active scene, the deleted bucket included
+    for (uint32_t k = 0; k < scenes_.size(); ++k) {
+        const SceneHost &s = scenes_[k];
+        if (!s.active) continue;
+        for (uint32_t c0 = 0; c0 <= s.desc.ncell; c0 += kCellTile) {
+            tile_scene_.push_back(k);
+            tile_start_.push_back(c0);
+        }
+    }
+    ctrl_.n_cell_tiles = (uint32_t)tile_scene_.size() - ctrl_.n_tiles;
     ctrl_.n_cells = (uint32_t)calloc_.high_water();
     ctrl_.n_scenes = (uint32_t)scenes_.size();
 }
@@ -635,6 +647,8 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.grid_omega = g(o.omega);
     sh.grid_apply = g(o.apply);
     sh.grid_xsph = g(o.xsph);
+    sh.grid_cells = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.cells),
+                                       std::max<uint32_t>(1, ctrl_.n_cell_tiles));
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan
@@ -668,6 +682,7 @@ StepArgs Batch::args() const
     a.wx = d_wx_;
     a.wpos = d_wpos_;
     a.dense = d_dense_;
+    a.mid = d_mid_;
     a.chist = d_chist_;
     a.id_tmp = d_id_tmp_;
     a.next_id = d_next_id_;

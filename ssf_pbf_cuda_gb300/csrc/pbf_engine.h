@@ -142,6 +142,7 @@ private:
     uint64_t *d_chist_ = nullptr;                     // per cell: class counts of its bucket
     uint32_t *d_wpos_ = nullptr;                      // sorted slot -> walk-copy slot
     uint32_t *d_dense_ = nullptr;                     // dense-bucket queue
+    uint32_t *d_mid_ = nullptr;                       // medium-bucket queue
     uint32_t *h_small_ = nullptr;     // pinned host scratch: pack offsets + counts
     cudaEvent_t small_done_ = nullptr;
     uint64_t bnd_capacity_ = 0;

@@ -56,16 +56,16 @@ static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
 // Device-resident launch control; lets a captured graph run on a scene set
 // that changes between launches.
 struct Ctrl {
-    uint32_t n_tiles;    // tiles in tile_scene/tile_start
-    uint32_t n_cells;    // cell entries to scan (high-water mark of cell ranges)
+    uint32_t n_tiles;       // particle tiles at the front of tile_scene/tile_start
+    uint32_t n_cells;       // cell entries to scan (high-water mark of cell ranges)
     uint32_t n_scenes;
-    uint32_t pad;
+    uint32_t n_cell_tiles;  // cell tiles after them: kCellTile cells of one scene each
 };
 
 struct StepArgs {
     const SceneDesc *scenes;
     const uint32_t *tile_scene;   // tile -> scene
-    const uint32_t *tile_start;   // tile -> first local particle index
+    const uint32_t *tile_start;   // tile -> first local particle index (cell tiles: first local cell)
     const Ctrl *ctrl;
     uint32_t *scene_num;          // particles per scene at step start
     uint32_t *flags;              // per-scene PBF_FLAG_* words
@@ -83,6 +83,7 @@ struct StepArgs {
     uint8_t *cls;                 // alias class of each particle (input order)
     uint32_t *wpos;               // sorted slot -> walk-copy slot (mixed-class buckets only)
     uint32_t *dense;              // [0] count, then (cell, scene) pairs of buckets for k_dense_sort
+    uint32_t *mid;                // the same for buckets of kMidMin+1 .. kDenseMin members
     float4 *wx;                   // walk copy of mixed-class buckets: grouped by class, .w = sorted slot
     uint64_t *chist;              // per cell: 8 x 8-bit class counts of its bucket, or kClassWhole
     uint32_t *next_id;            // per scene: id of the next particle added
@@ -96,9 +97,11 @@ struct LaunchShape {
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
+    uint32_t grid_cells;  // persistent grid of k_rank_cells (blocks of kCellTile threads)
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
+               grid_cells == o.grid_cells &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
@@ -106,7 +109,7 @@ struct LaunchShape {
 
 // Resident blocks per SM of each kernel class at a tile size / chunk.
 struct Occupancy {
-    uint32_t light, nb, lambda, dp, omega, apply, xsph;
+    uint32_t light, nb, lambda, dp, omega, apply, xsph, cells;
 };
 Occupancy occupancy(uint32_t tile, uint32_t chunk);
 
@@ -152,5 +155,7 @@ constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;
 constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells per scan tile
 constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
+constexpr uint32_t kCellTile = 256;         // cells per cell tile = threads per k_rank_cells block
+constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)
 
 }  // namespace pbf103

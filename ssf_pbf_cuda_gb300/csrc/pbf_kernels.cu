@@ -450,7 +450,8 @@ __global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         carry = 0;
-        *a.dense = 0;  // the dense-bucket queue of this step's k_rank_reorder
+        *a.dense = 0;  // the bucket queues of this step's k_rank_cells
+        *a.mid = 0;
     }
     __syncthreads();
     for (uint32_t base = 0; base < ntile; base += 1024) {
@@ -483,7 +484,8 @@ __global__ void __launch_bounds__(1024) k_scan_single(StepArgs a)
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         carry = 0;
-        *a.dense = 0;  // the dense-bucket queue of this step's k_rank_reorder
+        *a.dense = 0;  // the bucket queues of this step's k_rank_cells
+        *a.mid = 0;
     }
     __syncthreads();
     for (uint32_t base = 0; base < n; base += 1024) {
@@ -568,87 +570,86 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
     TILE_LOOP_END
 }
 
-// Stable rank inside the bucket (count of smaller input indices), then the
-// reorder of predicted and old positions (reorderDataCUDA x2,
-// pbf_neighbor_search_util.cu:143-154).  The result equals a stable sort by
-// cell (cub::DeviceRadixSort::SortPairs order).  Buckets larger than
-// kStableLimit keep the atomic order (PBF_FLAG_UNSTABLE_ORDER is not part of
-// the ABI; such buckets only arise from degenerate inputs or mass deletion).
+// Stable rank inside each bucket (count of smaller input indices): the
+// permutation of a stable sort by cell (cub::DeviceRadixSort::SortPairs
+// order), which reorderDataCUDA (pbf_neighbor_search_util.cu:143-154) then
+// applies.  One thread per cell, cells in order, so the cell ranges, the
+// bucket entries and the bucket's part of the permutation are read and
+// written contiguously whatever the particles' input order.  Buckets of up
+// to kMidMin members are ranked here; larger ones are queued for
+// k_dense_sort (a warp per bucket up to kDenseMin members, a block beyond).
+// Buckets larger than kStableLimit keep the atomic order (they only arise
+// from degenerate inputs or mass deletion).
 constexpr uint32_t kStableLimit = 4096;
-// Buckets with more members than kDenseMin (and at most kStableLimit) are
-// ordered by k_dense_sort (a block per bucket) instead of a member scan per
-// particle, which costs O(members^2) per bucket.
 constexpr uint32_t kDenseMin = 64;
-
-__global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
+__global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
 {
-    TILE_LOOP_BEGIN
-    const uint32_t n = a.scene_num[s];
-    if (local >= n) continue;
-    const SceneDesc d = a.scenes[s];
-    const uint32_t i = d.p_off + local;
-    const uint32_t gk = d.c_off + a.key[i];
-    const uint32_t st = a.offsets[gk], en = a.offsets[gk + 1];
-    // rank: members with a smaller input index (stable sorted order); for the
-    // walk copy also members of a smaller class, members of the same class
-    // with a smaller input index, and the bucket's class histogram
-    const bool packed = d.capacity <= kClsLimit;
-    const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
-    const uint32_t my_cls = a.cls[i];
-    uint32_t rank, below = 0, frank = 0;
-    const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
-    uint64_t hist = (uint64_t)(en - st) << (8u * my_cls);  // every member of my class
-    bool mixed = false;
-    if (en - st > kDenseMin && en - st <= kStableLimit) {
-        // a dense bucket: one block of k_dense_sort orders it; its first
-        // member by atomic slot queues it
-        if (a.slot[i] == 0) {
-            const uint32_t k = atomicAdd(a.dense, 1u);
-            a.dense[1 + 2 * k] = gk;
-            a.dense[2 + 2 * k] = s;
+    const uint32_t n0 = a.ctrl->n_tiles, nct = a.ctrl->n_cell_tiles;
+    for (uint32_t t_ = blockIdx.x; t_ < nct; t_ += gridDim.x) {
+        // the tile's scene: its fields once per tile, in registers
+        const uint32_t s = __ldg(a.tile_scene + n0 + t_);
+        const SceneDesc *sd = a.scenes + s;
+        const uint32_t ncell = __ldg(&sd->ncell), c_off = __ldg(&sd->c_off), p_off = __ldg(&sd->p_off);
+        const bool packed = __ldg(&sd->capacity) <= kClsLimit;
+        const bool grouped = packed && __ldg(&sd->gx) >= 4 && __ldg(&sd->gy) >= 4 && __ldg(&sd->gz) >= 4;
+        const uint32_t lc = __ldg(a.tile_start + n0 + t_) + threadIdx.x;
+        if (lc > ncell) continue;  // local cells 0..ncell (ncell: the deleted bucket)
+        const uint32_t gk = c_off + lc;
+        const uint32_t st = __ldg(a.offsets + gk), en = __ldg(a.offsets + gk + 1);
+        if (st == en) continue;
+        const uint32_t b = en - st;
+        if (b > kMidMin && b <= kStableLimit) {
+            uint32_t *q = b > kDenseMin ? a.dense : a.mid;
+            const uint32_t k = atomicAdd(q, 1u);
+            q[1 + 2 * k] = gk;
+            q[2 + 2 * k] = s;
+            continue;
         }
-        continue;
-    }
-    if (en - st <= kStableLimit) {
-        rank = 0;
-        uint32_t diff = 0;
-        for (uint32_t t = st; t < en; ++t) {
-            const uint32_t e = __ldg(a.tmp + t);
-            rank += ((e & imask) < local) ? 1u : 0u;
-            diff |= (e >> kClsShift) ^ my_cls;
-        }
-        if (grouped && diff) {  // several classes: the class histogram and my place in the walk copy
-            mixed = true;
-            hist = 0;
-            for (uint32_t t = st; t < en; ++t) {
-                const uint32_t e = __ldg(a.tmp + t);
-                const uint32_t mc = e >> kClsShift;
-                below += (mc < my_cls) ? 1u : 0u;
-                frank += (mc == my_cls && (e & imask) < local) ? 1u : 0u;
-                hist += 1ull << (8u * mc);
+        const uint32_t g0 = p_off + (st - __ldg(a.offsets + c_off));
+        const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
+        if (b > kStableLimit) {  // atomic order: entry t of the bucket came with slot t
+            for (uint32_t t = 0; t < b; ++t) {
+                a.perm[g0 + t] = __ldg(a.tmp + st + t) & imask;
+                a.wpos[g0 + t] = kNoWalkCopy;
             }
+            a.chist[gk] = kClassWhole;
+            continue;
         }
-    } else {
-        rank = a.slot[i];
+        // the alias class rides in the entries' top bits (scenes below 2^29
+        // particles); the walk copy groups a bucket by class when the grid
+        // is at least 4 cells on every axis
+        uint32_t e[kMidMin];
+        uint64_t hist = 0;
+        for (uint32_t t = 0; t < b; ++t) {
+            e[t] = __ldg(a.tmp + st + t);
+            hist += 1ull << (8u * (packed ? e[t] >> kClsShift : 0u));
+        }
+        const uint32_t c0 = packed ? e[0] >> kClsShift : 0u;
+        const bool mixed = grouped && hist != ((uint64_t)b << (8u * c0));
+        for (uint32_t t = 0; t < b; ++t) {
+            const uint32_t it = e[t] & imask, ct = packed ? e[t] >> kClsShift : 0u;
+            uint32_t rank = 0, below = 0, frank = 0;
+            for (uint32_t u = 0; u < b; ++u) {
+                const uint32_t iu = e[u] & imask, cu = packed ? e[u] >> kClsShift : 0u;
+                rank += iu < it ? 1u : 0u;
+                below += cu < ct ? 1u : 0u;
+                frank += (cu == ct && iu < it) ? 1u : 0u;
+            }
+            a.perm[g0 + rank] = it;
+            a.wpos[g0 + rank] = mixed ? g0 + below + frank : kNoWalkCopy;
+        }
+        a.chist[gk] = grouped ? hist : kClassWhole;
     }
-    const uint32_t base = a.offsets[d.c_off];
-    const uint32_t g = d.p_off + (st - base) + rank;
-    // only 4-byte entries are scattered here; k_gather moves the 16-byte
-    // particle data in sorted order (coalesced writes, as the reference's
-    // reorderDataCUDA gathers).  Buckets holding more than one alias class
-    // also place the particle in the class-grouped walk copy.
-    a.wpos[g] = mixed ? d.p_off + (st - base) + below + frank : kNoWalkCopy;
-    if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
-    a.perm[g] = local;
-    TILE_LOOP_END
 }
 
-// Dense buckets queued by k_rank_reorder, one block each: the members'
-// bucket entries (input index, alias class in the top bits) are sorted in
-// shared memory by input index (the stable sorted order) and, when the
-// bucket mixes classes, by (class, index) (the walk copy's order); the
-// results are the same permutation, class counts and walk-copy places the
-// per-particle member scan of k_rank_reorder produces.
+// Buckets queued by k_rank_cells.  Medium ones (kMidMin+1 .. kDenseMin
+// members) first, a warp each: members in lanes, each ranked by counting
+// over the others (broadcast by shuffle).  Dense ones (kDenseMin+1 ..
+// kStableLimit) then, a block each: the bucket entries (input index, alias
+// class in the top bits) are sorted in shared memory by input index (the
+// stable sorted order) and, when the bucket mixes classes, by (class, index)
+// (the walk copy's order).  Both give the permutation, class counts and
+// walk-copy places of k_rank_cells' per-bucket count.
 __device__ __forceinline__ uint32_t dense_key(uint32_t e, uint32_t imask)
 {
     return e == 0xFFFFFFFFu ? 0xFFFFFFFFu : (e & imask);  // padding sorts last
@@ -678,6 +679,48 @@ __global__ void __launch_bounds__(256) k_dense_sort(StepArgs a)
 {
     __shared__ uint32_t S[kStableLimit], W[kStableLimit];
     __shared__ uint32_t chist_cnt[8];
+    {
+        const uint32_t nm = *(volatile const uint32_t *)a.mid;
+        const uint32_t lane = threadIdx.x & 31u, wpb = blockDim.x >> 5;
+        for (uint32_t k = blockIdx.x * wpb + (threadIdx.x >> 5); k < nm; k += gridDim.x * wpb) {
+            const uint32_t gk = a.mid[1 + 2 * k], s = a.mid[2 + 2 * k];
+            const SceneDesc &d = a.scenes[s];
+            const uint32_t st = a.offsets[gk], b = a.offsets[gk + 1] - st;
+            const uint32_t g0 = d.p_off + (st - a.offsets[d.c_off]);
+            const bool packed = d.capacity <= kClsLimit;
+            const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
+            const bool grouped = packed && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+            const bool h0 = lane < b, h1 = 32u + lane < b;
+            const uint32_t e0 = h0 ? a.tmp[st + lane] : 0u, e1 = h1 ? a.tmp[st + 32u + lane] : 0u;
+            const uint32_t i0 = e0 & imask, i1 = e1 & imask;
+            const uint32_t c0 = packed ? e0 >> kClsShift : 0u, c1 = packed ? e1 >> kClsShift : 0u;
+            uint64_t hist = (h0 ? 1ull << (8u * c0) : 0ull) + (h1 ? 1ull << (8u * c1) : 0ull);
+#pragma unroll
+            for (uint32_t o = 16; o > 0; o >>= 1) hist += __shfl_xor_sync(0xffffffffu, hist, o);
+            const uint32_t cf = __shfl_sync(0xffffffffu, c0, 0);
+            const bool mixed = grouped && hist != ((uint64_t)b << (8u * cf));
+            uint32_t r0 = 0, b0 = 0, f0 = 0, r1 = 0, b1 = 0, f1 = 0;
+            for (uint32_t u = 0; u < b; ++u) {
+                const uint32_t eu = __shfl_sync(0xffffffffu, u < 32u ? e0 : e1, u & 31u);
+                const uint32_t iu = eu & imask, cu = packed ? eu >> kClsShift : 0u;
+                r0 += iu < i0 ? 1u : 0u;
+                b0 += cu < c0 ? 1u : 0u;
+                f0 += (cu == c0 && iu < i0) ? 1u : 0u;
+                r1 += iu < i1 ? 1u : 0u;
+                b1 += cu < c1 ? 1u : 0u;
+                f1 += (cu == c1 && iu < i1) ? 1u : 0u;
+            }
+            if (h0) {
+                a.perm[g0 + r0] = i0;
+                a.wpos[g0 + r0] = mixed ? g0 + b0 + f0 : kNoWalkCopy;
+            }
+            if (h1) {
+                a.perm[g0 + r1] = i1;
+                a.wpos[g0 + r1] = mixed ? g0 + b1 + f1 : kNoWalkCopy;
+            }
+            if (lane == 0) a.chist[gk] = grouped ? hist : kClassWhole;
+        }
+    }
     const uint32_t nd = *(volatile const uint32_t *)a.dense;
     for (uint32_t k = blockIdx.x; k < nd; k += gridDim.x) {
         const uint32_t gk = a.dense[1 + 2 * k], s = a.dense[2 + 2 * k];
@@ -1231,7 +1274,8 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
     Occupancy o;
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
-                 mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
+                 mn(occ((const void *)k_gather), occ((const void *)k_finalize)));
+    o.cells = occ_b((const void *)k_rank_cells, kCellTile);
     o.nb = occ((const void *)k_neighbors_lambda);
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
@@ -1291,8 +1335,8 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     }
     k_scatter<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_scatter");
-    k_rank_reorder<<<g, b, 0, st>>>(a);
-    PBF_LAUNCHED("k_rank_reorder");
+    k_rank_cells<<<sh.grid_cells, kCellTile, 0, st>>>(a);
+    PBF_LAUNCHED("k_rank_cells");
     k_dense_sort<<<sh.grid, 256, 0, st>>>(a);
     PBF_LAUNCHED("k_dense_sort");
     k_gather<<<g, b, 0, st>>>(a);

@@ -154,7 +154,7 @@ def test_profile_step_names_every_kernel(gpu):
     names = [n for n, _ in prof]
     # small tables are scanned by one block, larger ones in three phases
     scan = ["k_scan_single"] if names[1] == "k_scan_single" else ["k_scan_reduce", "k_scan_spine", "k_scan_down"]
-    head = ["k_predict_hash", *scan, "k_scatter", "k_rank_reorder", "k_dense_sort", "k_gather", "k_neighbors_lambda"]
+    head = ["k_predict_hash", *scan, "k_scatter", "k_rank_cells", "k_dense_sort", "k_gather", "k_neighbors_lambda"]
     assert names[:len(head)] == head
     assert names.count("k_dp") == 4 and names.count("k_lambda") == 3
     assert b.launches == len(prof)
