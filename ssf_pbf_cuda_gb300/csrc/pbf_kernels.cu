@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 // per-pair cache: W and grad W are recomputed from positions).  One thread
 // per particle; the neighbour sums run in list order.
 template <int kChunk>
-__global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, const float4 *__restrict__ xc)
+__global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restrict__ xc)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
@@ -889,7 +889,9 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, const float4 *__r
     });
     const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
     const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    // lambda rides in .w of the positions this pass reads and the delta-p
+    // pass gathers next (neighbours here use only .xyz)
+    reinterpret_cast<float *>(xc + i)[3] = C / fmaf(d.m2rho2, K, d.relax);
     TILE_LOOP_END
 }
 
@@ -898,7 +900,7 @@ enum ScorrForm { kScorrReference, kScorrTextbook, kScorrOff, kScorrTextbook4 };
 
 // Sum over the list of -(lambda_i + lambda_j + s_corr) grad W (the body of
 // calcPositionUpdateCUDA, pbf_position_update.cu:131-188).
-template <int kChunk, int FORM>
+template <int kChunk, int FORM, bool LAMW>
 __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, const float4 *__restrict__ xc,
                                          uint32_t i, float4 xp, float li)
 {
@@ -909,8 +911,9 @@ __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, 
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
-        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
-        const float lj = __ldg(lam + q);
+        const float4 xq = __ldg(xc + q);
+        const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
+        const float lj = LAMW ? xq.w : __ldg(lam + q);  // LAMW: lambda in .w of the positions
         float corr = 0.f;
         if (FORM == kScorrReference) {
             const float kr2 = pk.W * pk.W;
@@ -939,7 +942,7 @@ __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, 
 // buffer so neighbours still read the old positions.  On the last iteration
 // the velocity update (updateVelocityCUDA, pbf_update.cu:25-39) is fused in:
 // v = (x_new - x_old) / dt, written with x_new to the particle phase.
-template <int kChunk>
+template <int kChunk, bool LAMW>
 __global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restrict__ xc, float4 *__restrict__ xo,
                                                float4 *__restrict__ vo, int last)
 {
@@ -951,16 +954,16 @@ __global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restr
     if (local >= live) continue;
     const uint32_t i = d.p_off + local;
     const float4 xp = xc[i];
-    const float li = a.lam[i];
+    const float li = LAMW ? xp.w : a.lam[i];
     float3 sum;
     if (d.tensile_mode == PBF_TENSILE_REFERENCE)
-        sum = dp_sum<kChunk, kScorrReference>(a, d, xc, i, xp, li);
+        sum = dp_sum<kChunk, kScorrReference, LAMW>(a, d, xc, i, xp, li);
     else if (d.tensile_mode == PBF_TENSILE_TEXTBOOK && d.scorr_n == 4)
-        sum = dp_sum<kChunk, kScorrTextbook4>(a, d, xc, i, xp, li);
+        sum = dp_sum<kChunk, kScorrTextbook4, LAMW>(a, d, xc, i, xp, li);
     else if (d.tensile_mode == PBF_TENSILE_TEXTBOOK)
-        sum = dp_sum<kChunk, kScorrTextbook>(a, d, xc, i, xp, li);
+        sum = dp_sum<kChunk, kScorrTextbook, LAMW>(a, d, xc, i, xp, li);
     else
-        sum = dp_sum<kChunk, kScorrOff>(a, d, xc, i, xp, li);
+        sum = dp_sum<kChunk, kScorrOff, LAMW>(a, d, xc, i, xp, li);
     float3 dp = make_float3(sum.x * d.m * d.inv_rho0, sum.y * d.m * d.inv_rho0, sum.z * d.m * d.inv_rho0);
     const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
     if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
@@ -1246,15 +1249,19 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 template <int CH>
 struct PassFns {
     static const void *lambda() { return (const void *)k_lambda<CH>; }
-    static const void *dp() { return (const void *)k_dp<CH>; }
-    static void launch_lambda(const StepArgs &a, const LaunchShape &sh, const float4 *cur, cudaStream_t st)
+    static const void *dp() { return (const void *)k_dp<CH, true>; }
+    static void launch_lambda(const StepArgs &a, const LaunchShape &sh, float4 *cur, cudaStream_t st)
     {
         k_lambda<CH><<<sh.grid_lambda, sh.tile, 0, st>>>(a, cur);
     }
+    // lamw: lambda in .w of cur (iterations >= 1); iteration 0 reads it from lam
     static void launch_dp(const StepArgs &a, const LaunchShape &sh, const float4 *cur, float4 *out, float4 *vo,
-                          int last, cudaStream_t st)
+                          int last, bool lamw, cudaStream_t st)
     {
-        k_dp<CH><<<sh.grid_dp, sh.tile, 0, st>>>(a, cur, out, vo, last);
+        if (lamw)
+            k_dp<CH, true><<<sh.grid_dp, sh.tile, 0, st>>>(a, cur, out, vo, last);
+        else
+            k_dp<CH, false><<<sh.grid_dp, sh.tile, 0, st>>>(a, cur, out, vo, last);
     }
 };
 
@@ -1353,7 +1360,7 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        PBF_PASS_DISPATCH(sh.chunk, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, st));
+        PBF_PASS_DISPATCH(sh.chunk, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, it > 0, st));
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;
