@@ -218,32 +218,58 @@ def run_serving(api, args, device: int) -> dict:
         del srv
         return comps, st, wall
 
-    # the rate that saturates the device: the server's busy throughput on a
-    # burst of requests (all queued at once) over the mean work of a request,
-    # E[N] E[horizon] with N log-uniform in [8192, 262144], horizon uniform in
-    # [60, 600]
+    # the rate that saturates the device, found by a ramp: start from the
+    # server's busy throughput on a burst of requests (all queued at once)
+    # over the mean work of a request, E[N] E[horizon] with N log-uniform in
+    # [8192, 262144] and horizon uniform in [60, 600]; raise the rate while
+    # the backlog stays bounded.  The HBM budget admits every request at
+    # once here, so an overload shows as completion latency growing with the
+    # rate rather than as admission wait: bounded = p99 completion latency
+    # within 2 s.  Report the last bounded rate (and the whole ramp).
     mean_n = (262144 - 8192) / math.log(262144 / 8192)
     mean_work = mean_n * (60 + 600) / 2
     _, st_cal, _ = serve(scenes.config5_requests(24, 1e6, seed_id=55))
     busy_tp = st_cal["particle_steps"] / max(st_cal["busy_s"], 1e-9)
-    rate = args.serve_rate if args.serve_rate > 0 else busy_tp / mean_work
-    n_req = max(1, int(rate * args.serve_seconds))
-    comps, st, wall = serve(scenes.config5_requests(n_req, rate))
-    lat = np.array(sorted(c["complete_s"] - c["arrival_s"] for c in comps))
-    qd = np.array(sorted(c["admit_s"] - c["arrival_s"] for c in comps))
-    return {
-        "requests": len(comps), "arrival_rate_hz": rate, "arrival_window_s": args.serve_seconds,
-        "rate_rule": "saturating: burst busy throughput / mean request work" if args.serve_rate <= 0 else "fixed",
-        "burst_busy_particle_steps_per_s": busy_tp,
-        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-        "p99_queue_s": float(np.percentile(qd, 99)),
-        "particle_steps_per_s": st["particle_steps"] / wall, "busy_particle_steps_per_s":
-            st["particle_steps"] / max(st["busy_s"], 1e-9),
-        "substeps": st["substeps"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9,
-        "hbm_budget_GB": 150, "wall_s": wall,
+
+    def run_at(rate, window):
+        n_req = max(1, int(rate * window))
+        comps, st, wall = serve(scenes.config5_requests(n_req, rate))
+        lat = np.array(sorted(c["complete_s"] - c["arrival_s"] for c in comps))
+        qd = np.array(sorted(c["admit_s"] - c["arrival_s"] for c in comps))
+        return {
+            "requests": len(comps), "arrival_rate_hz": rate, "arrival_window_s": window,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "p99_queue_s": float(np.percentile(qd, 99)),
+            "particle_steps_per_s": st["particle_steps"] / wall,
+            "busy_particle_steps_per_s": st["particle_steps"] / max(st["busy_s"], 1e-9),
+            "substeps": st["substeps"], "peak_resident_GB": st["peak_resident_bytes"] / 1e9, "wall_s": wall,
+        }
+
+    if args.serve_rate > 0:
+        best = run_at(args.serve_rate, args.serve_seconds)
+        ramp, rule = [best], "fixed"
+    else:
+        base = busy_tp / mean_work
+        ramp, best = [], None
+        for f in (1.0, 1.5, 2.0, 3.0):
+            r = run_at(base * f, args.serve_seconds)
+            ramp.append(r)
+            if r["p99_latency_s"] > 2.0 or r["p99_queue_s"] > 0.5:
+                break
+            best = r
+        best = best or ramp[0]
+        rule = ("ramp: the highest of 1, 1.5, 2, 3 x (burst busy throughput / mean request work) with p99 "
+                "completion latency <= 2 s and p99 admission wait <= 0.5 s")
+    out = dict(best)
+    out.update({
+        "rate_rule": rule, "burst_busy_particle_steps_per_s": busy_tp, "hbm_budget_GB": 150,
+        "ramp": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()
+                  if k in ("arrival_rate_hz", "particle_steps_per_s", "p50_latency_s", "p99_latency_s", "p99_queue_s",
+                           "peak_resident_GB")} for r in ramp],
         "workload": "dam-break requests, N log-uniform 8k-256k, horizons 60-600 steps, Poisson arrivals, "
                     "configured physics with s_corr k=1e-4",
-    }
+    })
+    return out
 
 
 SORT_KERNELS = ("k_predict_hash", "k_scan_reduce", "k_scan_spine", "k_scan_down", "k_scan_single", "k_scatter",
@@ -409,7 +435,8 @@ def main():
                     help="seconds of untimed steps before the warm-up: a GPU coming out of idle runs the first "
                          "seconds ~5%% slower")
     ap.add_argument("--chunk", type=int, default=0, help="neighbour chunk of the lambda/dp passes (0 = autotune)")
-    ap.add_argument("--serve-seconds", type=float, default=8.0, help="arrival window of the serving run (0 = off)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="arrival window of each serving run of the rate ramp (0 = off)")
     ap.add_argument("--serve-rate", type=float, default=0.0,
                     help="request arrivals per second (0 = the rate that saturates the device)")
     ap.add_argument("--serve-tile", type=int, default=256)
