@@ -273,7 +273,7 @@ def run_serving(api, args, device: int) -> dict:
 
 
 SORT_KERNELS = ("k_predict_hash", "k_scan_reduce", "k_scan_spine", "k_scan_down", "k_scan_single", "k_scatter",
-                "k_rank_cells", "k_dense_sort", "k_gather")
+                "k_rank_cells", "k_rank_reorder", "k_dense_sort", "k_gather")
 
 
 def run_ns_microbench(api, device: int, reps: int = 3) -> dict:

@@ -98,10 +98,12 @@ struct LaunchShape {
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
     uint32_t grid_cells;  // persistent grid of k_rank_cells (blocks of kCellTile threads)
+    uint32_t small;       // latency-bound step (at most kSmallStep particle slots): per-particle
+                          // rank, lambda kept in its own array
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
-               grid_cells == o.grid_cells &&
+               grid_cells == o.grid_cells && small == o.small &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
@@ -157,5 +159,6 @@ constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells pe
 constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
 constexpr uint32_t kCellTile = 256;         // cells per cell tile = threads per k_rank_cells block
 constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)
+constexpr uint32_t kSmallStep = 131072;     // particle slots up to which a step is latency bound
 
 }  // namespace pbf103

@@ -642,6 +642,74 @@ __global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
     }
 }
 
+// The same ranks from the particle side, for small steps (latency bound:
+// the per-cell kernel's b^2 loop in one thread lengthens the critical
+// path): each particle counts the smaller input indices of its bucket.
+// Buckets above kDenseMin members are queued for k_dense_sort by their
+// first member (atomic slot 0); nothing is queued for the warp tier.
+__global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
+{
+    TILE_LOOP_BEGIN
+    const uint32_t n = a.scene_num[s];
+    if (local >= n) continue;
+    const SceneDesc d = a.scenes[s];
+    const uint32_t i = d.p_off + local;
+    const uint32_t gk = d.c_off + a.key[i];
+    const uint32_t st = a.offsets[gk], en = a.offsets[gk + 1];
+    // rank: members with a smaller input index (stable sorted order); for the
+    // walk copy also members of a smaller class, members of the same class
+    // with a smaller input index, and the bucket's class histogram
+    const bool packed = d.capacity <= kClsLimit;
+    const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
+    const uint32_t my_cls = a.cls[i];
+    uint32_t rank, below = 0, frank = 0;
+    const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
+    uint64_t hist = (uint64_t)(en - st) << (8u * my_cls);  // every member of my class
+    bool mixed = false;
+    if (en - st > kDenseMin && en - st <= kStableLimit) {
+        // a dense bucket: one block of k_dense_sort orders it; its first
+        // member by atomic slot queues it
+        if (a.slot[i] == 0) {
+            const uint32_t k = atomicAdd(a.dense, 1u);
+            a.dense[1 + 2 * k] = gk;
+            a.dense[2 + 2 * k] = s;
+        }
+        continue;
+    }
+    if (en - st <= kStableLimit) {
+        rank = 0;
+        uint32_t diff = 0;
+        for (uint32_t t = st; t < en; ++t) {
+            const uint32_t e = __ldg(a.tmp + t);
+            rank += ((e & imask) < local) ? 1u : 0u;
+            diff |= (e >> kClsShift) ^ my_cls;
+        }
+        if (grouped && diff) {  // several classes: the class histogram and my place in the walk copy
+            mixed = true;
+            hist = 0;
+            for (uint32_t t = st; t < en; ++t) {
+                const uint32_t e = __ldg(a.tmp + t);
+                const uint32_t mc = e >> kClsShift;
+                below += (mc < my_cls) ? 1u : 0u;
+                frank += (mc == my_cls && (e & imask) < local) ? 1u : 0u;
+                hist += 1ull << (8u * mc);
+            }
+        }
+    } else {
+        rank = a.slot[i];
+    }
+    const uint32_t base = a.offsets[d.c_off];
+    const uint32_t g = d.p_off + (st - base) + rank;
+    // only 4-byte entries are scattered here; k_gather moves the 16-byte
+    // particle data in sorted order (coalesced writes, as the reference's
+    // reorderDataCUDA gathers).  Buckets holding more than one alias class
+    // also place the particle in the class-grouped walk copy.
+    a.wpos[g] = mixed ? d.p_off + (st - base) + below + frank : kNoWalkCopy;
+    if (rank == 0) a.chist[gk] = grouped ? hist : kClassWhole;
+    a.perm[g] = local;
+    TILE_LOOP_END
+}
+
 // Buckets queued by k_rank_cells.  Medium ones (kMidMin+1 .. kDenseMin
 // members) first, a warp each: members in lanes, each ranked by counting
 // over the others (broadcast by shuffle).  Dense ones (kDenseMin+1 ..
@@ -867,7 +935,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 // pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
 // per-pair cache: W and grad W are recomputed from positions).  One thread
 // per particle; the neighbour sums run in list order.
-template <int kChunk>
+template <int kChunk, bool LAMW>
 __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restrict__ xc)
 {
     TILE_LOOP_BEGIN
@@ -889,9 +957,15 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     });
     const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
     const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-    // lambda rides in .w of the positions this pass reads and the delta-p
-    // pass gathers next (neighbours here use only .xyz)
-    reinterpret_cast<float *>(xc + i)[3] = C / fmaf(d.m2rho2, K, d.relax);
+    // LAMW: lambda rides in .w of the positions this pass reads and the
+    // delta-p pass gathers next (neighbours here use only .xyz); small,
+    // latency-bound steps keep it in its own array, as the store into the
+    // gathered array slows this pass's neighbour reads there
+    const float lam = C / fmaf(d.m2rho2, K, d.relax);
+    if (LAMW)
+        reinterpret_cast<float *>(xc + i)[3] = lam;
+    else
+        a.lam[i] = lam;
     TILE_LOOP_END
 }
 
@@ -1248,11 +1322,14 @@ __global__ void k_f4_to_aos3(const float4 *__restrict__ src, float *__restrict__
 // The lambda / delta-p variants by neighbour chunk, selected at run time.
 template <int CH>
 struct PassFns {
-    static const void *lambda() { return (const void *)k_lambda<CH>; }
+    static const void *lambda() { return (const void *)k_lambda<CH, true>; }
     static const void *dp() { return (const void *)k_dp<CH, true>; }
-    static void launch_lambda(const StepArgs &a, const LaunchShape &sh, float4 *cur, cudaStream_t st)
+    static void launch_lambda(const StepArgs &a, const LaunchShape &sh, float4 *cur, bool lamw, cudaStream_t st)
     {
-        k_lambda<CH><<<sh.grid_lambda, sh.tile, 0, st>>>(a, cur);
+        if (lamw)
+            k_lambda<CH, true><<<sh.grid_lambda, sh.tile, 0, st>>>(a, cur);
+        else
+            k_lambda<CH, false><<<sh.grid_lambda, sh.tile, 0, st>>>(a, cur);
     }
     // lamw: lambda in .w of cur (iterations >= 1); iteration 0 reads it from lam
     static void launch_dp(const StepArgs &a, const LaunchShape &sh, const float4 *cur, float4 *out, float4 *vo,
@@ -1281,7 +1358,7 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
     Occupancy o;
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
-                 mn(occ((const void *)k_gather), occ((const void *)k_finalize)));
+                 mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
     o.cells = occ_b((const void *)k_rank_cells, kCellTile);
     o.nb = occ((const void *)k_neighbors_lambda);
     const bool c4 = chunk == 4;
@@ -1342,8 +1419,13 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     }
     k_scatter<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_scatter");
-    k_rank_cells<<<sh.grid_cells, kCellTile, 0, st>>>(a);
-    PBF_LAUNCHED("k_rank_cells");
+    if (sh.small) {
+        k_rank_reorder<<<g, b, 0, st>>>(a);
+        PBF_LAUNCHED("k_rank_reorder");
+    } else {
+        k_rank_cells<<<sh.grid_cells, kCellTile, 0, st>>>(a);
+        PBF_LAUNCHED("k_rank_cells");
+    }
     k_dense_sort<<<sh.grid, 256, 0, st>>>(a);
     PBF_LAUNCHED("k_dense_sort");
     k_gather<<<g, b, 0, st>>>(a);
@@ -1355,12 +1437,13 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     float4 *cur = a.xa, *nxt = a.xb;
     for (int it = 0; it < iters; ++it) {
         if (it > 0) {
-            PBF_PASS_DISPATCH(sh.chunk, launch_lambda(a, sh, cur, st));
+            PBF_PASS_DISPATCH(sh.chunk, launch_lambda(a, sh, cur, !sh.small, st));
             PBF_LAUNCHED("k_lambda");
         }
         const bool last = (it == iters - 1);
         float4 *out = last ? a.x : nxt;
-        PBF_PASS_DISPATCH(sh.chunk, launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, it > 0, st));
+        PBF_PASS_DISPATCH(sh.chunk,
+                          launch_dp(a, sh, cur, out, last ? vfinal : nullptr, last ? 1 : 0, it > 0 && !sh.small, st));
         PBF_LAUNCHED("k_dp");
         float4 *t = cur;
         cur = nxt;

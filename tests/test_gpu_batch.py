@@ -66,6 +66,34 @@ def test_batch_matches_oracle_per_scene(oracle, gpu):
         assert np.abs(v - r["v"]).max(initial=0) <= H.vel_abs_tol(p["time_step"], r["x"])
 
 
+def test_small_and_large_step_paths_agree(oracle, gpu):
+    """Steps of at most 131,072 particle slots are latency bound: they rank
+    each bucket from the particle side and keep lambda in its own array.
+    Larger steps rank per cell and carry lambda in the positions' w lane.
+    The same scene stepped alone (small) and inside a 163,840-particle batch
+    (large) gives bit-identical results, and the large path matches the
+    oracle."""
+    p = api.config_params(scorr_k=1e-4)
+    items = [(scenes.dam_break(32, 32, 32, (4.0, 2.0, 2.0), scene_id=41 + k), p) for k in range(5)]
+    b, ids = make_batch(items)
+    for _ in range(2):
+        b.step(4)
+    sc = items[0][0]
+    x, v = b.get_scene(ids[0])
+    a = alone(sc, p, 2)
+    assert np.array_equal(x, a["x"]) and np.array_equal(v, a["v"])
+    b2, ids2 = make_batch(items[:1])
+    b2.step(4)
+    x1, v1 = b2.get_scene(ids2[0])
+    b3, ids3 = make_batch(items)
+    b3.step(4)
+    xl, vl = b3.get_scene(ids3[0])
+    assert np.array_equal(x1, xl) and np.array_equal(v1, vl)
+    r = H.run_oracle(oracle, sc, p, "planes", 4, f64=True)
+    assert H.pos_rel_err(xl, r["x"]) <= H.POS_RTOL
+    assert np.abs(vl - r["v"]).max(initial=0) <= H.vel_abs_tol(p["time_step"], r["x"])
+
+
 @pytest.mark.parametrize("tile", [64, 128, 256, 512])
 def test_tile_sizes_give_identical_results(gpu, tile):
     items = mixed_scenes()[:3]
@@ -154,7 +182,9 @@ def test_profile_step_names_every_kernel(gpu):
     names = [n for n, _ in prof]
     # small tables are scanned by one block, larger ones in three phases
     scan = ["k_scan_single"] if names[1] == "k_scan_single" else ["k_scan_reduce", "k_scan_spine", "k_scan_down"]
-    head = ["k_predict_hash", *scan, "k_scatter", "k_rank_cells", "k_dense_sort", "k_gather", "k_neighbors_lambda"]
+    # small (latency-bound) steps rank per particle, larger ones per cell
+    rank = "k_rank_reorder" if "k_rank_reorder" in names else "k_rank_cells"
+    head = ["k_predict_hash", *scan, "k_scatter", rank, "k_dense_sort", "k_gather", "k_neighbors_lambda"]
     assert names[:len(head)] == head
     assert names.count("k_dp") == 4 and names.count("k_lambda") == 3
     assert b.launches == len(prof)
