@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(512) k_predict_hash(StepArgs a)
     ps.x = __fmaf_rn(__fmaf_rn(d.g[0], dt, vv.x), dt, xv.x);
     ps.y = __fmaf_rn(__fmaf_rn(d.g[1], dt, vv.y), dt, xv.y);
     ps.z = __fmaf_rn(__fmaf_rn(d.g[2], dt, vv.z), dt, xv.z);
-    ps.w = 0.f;
+    ps.w = __uint_as_float(a.id[i]);  // the id travels with the prediction to k_gather
     const int32_t cx = cell_coord(ps.x, d.cw), cy = cell_coord(ps.y, d.cw), cz = cell_coord(ps.z, d.cw);
     uint32_t key = hash3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz, d);
     uint32_t cls = alias_class(cx, cy, cz, d);
@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(512) k_gather(StepArgs a)
     const float4 xg = make_float4(ps.x, ps.y, ps.z, __uint_as_float(g));
     a.xa[g] = xg;
     a.xold[g] = a.x[i];
-    a.id_tmp[g] = a.id[i];
+    a.id_tmp[g] = __float_as_uint(ps.w);  // the id, stored beside the prediction
     const uint32_t w = a.wpos[g];
     if (w != kNoWalkCopy) a.wx[w] = xg;
     TILE_LOOP_END
