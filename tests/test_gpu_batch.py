@@ -138,6 +138,36 @@ def test_set_all_get_all_roundtrip(gpu):
     assert np.array_equal(x2, x + np.float32(0.001)) and np.array_equal(v2, v + np.float32(0.5))
 
 
+def test_pinned_and_pageable_host_buffers_agree(gpu):
+    """Packed host buffers in page-locked (pinned) and in pageable memory
+    give the same bits, in both directions, around a step."""
+    import torch
+    items = mixed_scenes()
+    counts = np.array([sc.n for sc, _ in items], np.uint32)
+    x0 = np.concatenate([sc.x for sc, _ in items]) + np.float32(0.002)
+    v0 = np.concatenate([sc.v for sc, _ in items]) + np.float32(0.25)
+    xp = torch.from_numpy(x0.copy()).pin_memory()
+    vp = torch.from_numpy(v0.copy()).pin_memory()
+    out = []
+    for pinned in (False, True):
+        b, _ = make_batch(items)
+        if pinned:
+            b.set_all(xp.numpy(), vp.numpy(), counts)
+        else:
+            b.set_all(x0, v0, counts)
+        b.step(4)
+        if pinned:
+            xo = torch.zeros_like(xp).pin_memory()
+            vo = torch.zeros_like(vp).pin_memory()
+            c, _, _ = b.get_all(xo.numpy(), vo.numpy())
+            out.append((np.asarray(c), xo.numpy().copy(), vo.numpy().copy()))
+        else:
+            out.append(b.get_all())
+    assert np.array_equal(out[0][0], out[1][0])
+    n = int(np.sum(out[0][0]))
+    assert np.array_equal(out[0][1][:n], out[1][1][:n]) and np.array_equal(out[0][2][:n], out[1][2][:n])
+
+
 def test_autotune_preserves_state(gpu):
     items = mixed_scenes()
     b, ids = make_batch(items)
