@@ -98,12 +98,13 @@ struct LaunchShape {
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
     uint32_t grid_cells;  // persistent grid of k_rank_cells (blocks of kCellTile threads)
-    uint32_t small;       // latency-bound step (at most kSmallStep particle slots): per-particle
-                          // rank, lambda kept in its own array
+    uint32_t small;       // latency-bound step (at most kSmallStep particle slots): split
+                          // neighbour walk, per-particle rank, lambda kept in its own array
+    uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 64 particles each)
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
-               grid_cells == o.grid_cells && small == o.small &&
+               grid_cells == o.grid_cells && small == o.small && grid_split == o.grid_split &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
@@ -111,7 +112,7 @@ struct LaunchShape {
 
 // Resident blocks per SM of each kernel class at a tile size / chunk.
 struct Occupancy {
-    uint32_t light, nb, lambda, dp, omega, apply, xsph, cells;
+    uint32_t light, nb, lambda, dp, omega, apply, xsph, cells, split;
 };
 Occupancy occupancy(uint32_t tile, uint32_t chunk);
 

@@ -244,7 +244,8 @@ __device__ __forceinline__ void walk27_ranges(const SceneDesc &d, const uint32_t
 template <bool PRUNE, class R>
 __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t *__restrict__ offsets,
                                              const uint64_t *__restrict__ chist, const float4 *xa,
-                                             const float4 *wx, uint32_t shift, float4 xp, R &&r)
+                                             const float4 *wx, uint32_t shift, float4 xp, R &&r, int rr0 = 0,
+                                             int rr1 = 9)
 {
     const int32_t icx = cell_coord(xp.x, d.cw), icy = cell_coord(xp.y, d.cw), icz = cell_coord(xp.z, d.cw);
     const bool prune = PRUNE && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
@@ -262,7 +263,7 @@ __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t 
     const uint32_t *off = offsets + d.c_off;
     const uint64_t *ch = chist + d.c_off;
 #pragma unroll 1
-    for (int rr = 0; rr < 9; ++rr) {
+    for (int rr = rr0; rr < rr1; ++rr) {  // rows (dz, dy), z outermost: the reference's walk order
         const int dz = rr / 3 - 1, dy = rr % 3 - 1;
         bool left = true, right = true;
         if (prune) {
@@ -931,6 +932,114 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     TILE_LOOP_END
 }
 
+// Small (latency-bound) steps: one particle's walk split over kSplit lanes
+// of a warp, each walking a contiguous run of the nine (dz, dy) rows into a
+// private buffer of at most cap entries.  A prefix over the group's counts
+// then places every lane's entries after those of the rows before it, so the
+// list holds the first cap accepted candidates in the reference's walk
+// order, as k_neighbors_lambda's.  The particle's first lane then sums the
+// iteration-0 lambda over the list in list order (the same sum, bit for
+// bit).  Scenes with more than kSplitCap list slots walk in one lane.
+constexpr uint32_t kSplit = 4;
+constexpr uint32_t kSplitCap = 64;
+__global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t tile)
+{
+    const uint32_t per_block = blockDim.x / kSplit;  // particles per block
+    const uint32_t parts = tile / per_block;         // blocks per tile
+    const uint32_t lane = threadIdx.x & 31u, sub = threadIdx.x % kSplit;
+    const uint32_t gmask = 0xFu << (lane & ~3u);    // the particle's kSplit lanes
+    const uint32_t n_work = a.ctrl->n_tiles * parts;
+    for (uint32_t u = blockIdx.x; u < n_work; u += gridDim.x) {
+        const uint32_t t_ = u / parts;
+        const uint32_t s = __ldg(a.tile_scene + t_);
+        const uint32_t local = __ldg(a.tile_start + t_) + (u % parts) * per_block + threadIdx.x / kSplit;
+        const SceneDesc d = a.scenes[s];
+        const uint32_t base = a.offsets[d.c_off];
+        const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
+        if (local >= live) continue;  // the same for the group's lanes
+        const uint32_t i = d.p_off + local;
+        const uint32_t shift = d.p_off - base;
+        const float4 xp = a.xa[i];
+        const float h2 = d.h2;
+        const uint32_t cap = d.cap;
+        const uint64_t stride = a.nbr_stride;
+        uint32_t *nl = a.nbr + i;
+        const float4 *__restrict__ xa = a.xa;
+        const float4 *__restrict__ wx = a.wx;
+        // rows {0,1,2} {3,4} {5,6} {7,8}; one lane takes all nine when the
+        // list does not fit the private buffer
+        const bool one = cap > kSplitCap;
+        const int rr0 = one ? (sub == 0 ? 0 : 9) : (sub == 0 ? 0 : 1 + 2 * (int)sub);
+        const int rr1 = one ? (sub == 0 ? 9 : 9) : 3 + 2 * (int)sub;
+        uint32_t buf[kSplitCap];
+        uint32_t cnt = 0;
+        if (one && sub == 0) {  // write straight into the list
+            walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
+                               [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
+                for (uint32_t q = st; q < en; ++q) {
+                    const float4 c = __ldg(src + q);
+                    if (dist2_exact(xp, c) < h2) {
+                        nl[(uint64_t)cnt * stride] = __float_as_uint(c.w);
+                        if (++cnt == cap) return false;
+                    }
+                }
+                return true;
+            });
+        } else if (!one) {
+            walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
+                               [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
+                for (uint32_t q0 = st; q0 < en; q0 += 4) {
+                    float4 c[4];
+#pragma unroll
+                    for (uint32_t k = 0; k < 4; ++k)
+                        if (q0 + k < en) c[k] = __ldg(src + q0 + k);
+#pragma unroll
+                    for (uint32_t k = 0; k < 4; ++k) {
+                        if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
+                            buf[cnt] = __float_as_uint(c[k].w);
+                            if (++cnt == cap) return false;
+                        }
+                    }
+                }
+                return true;
+            }, rr0, rr1);
+        }
+        // place the group's runs one after the other, up to cap
+        uint32_t incl = cnt;
+#pragma unroll
+        for (uint32_t o = 1; o < kSplit; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(gmask, incl, o, kSplit);
+            if (sub >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(gmask, incl, kSplit - 1, kSplit);
+        if (!one) {
+            const uint32_t pre = incl - cnt;
+            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) nl[(uint64_t)(pre + t) * stride] = buf[t];
+        }
+        const uint32_t nn = total < cap ? total : cap;
+        __syncwarp(gmask);  // the list entries of the group are visible to its first lane
+        if (sub != 0) continue;
+        a.nnb[i] = (uint8_t)nn;
+        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+        float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+        const uint32_t *rd = nl;
+#pragma unroll 4
+        for (uint32_t k = 0; k < nn; ++k) {
+            const uint32_t q = *rd;
+            rd += stride;
+            const PairK pk = pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta);
+            ks += pk.W;
+            g0 += pk.gx;
+            g1 += pk.gy;
+            g2 += pk.gz;
+            kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+        }
+        const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
+        const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+        a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    }
+}
+
 // lambda for iterations >= 1 (memorizeKernelCalc + calcScalingFactor,
 // pbf_kernel_memorization.cu:93-134 and pbf_constraint.cu:168-209, without the
 // per-pair cache: W and grad W are recomputed from positions).  One thread
@@ -1360,6 +1469,7 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
                  mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
     o.cells = occ_b((const void *)k_rank_cells, kCellTile);
+    o.split = occ_b((const void *)k_neighbors_split, 256);
     o.nb = occ((const void *)k_neighbors_lambda);
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
@@ -1430,8 +1540,13 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     PBF_LAUNCHED("k_dense_sort");
     k_gather<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_gather");
-    k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
-    PBF_LAUNCHED("k_neighbors_lambda");
+    if (sh.small) {
+        k_neighbors_split<<<sh.grid_split, 256, 0, st>>>(a, sh.tile);
+        PBF_LAUNCHED("k_neighbors_split");
+    } else {
+        k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
+        PBF_LAUNCHED("k_neighbors_lambda");
+    }
     const bool xsph = (post & (kPostXsphWalk | kPostXsphList)) != 0;
     float4 *vfinal = xsph ? a.vt : a.v;
     float4 *cur = a.xa, *nxt = a.xb;

@@ -212,9 +212,12 @@ def test_profile_step_names_every_kernel(gpu):
     names = [n for n, _ in prof]
     # small tables are scanned by one block, larger ones in three phases
     scan = ["k_scan_single"] if names[1] == "k_scan_single" else ["k_scan_reduce", "k_scan_spine", "k_scan_down"]
-    # small (latency-bound) steps rank per particle, larger ones per cell
-    rank = "k_rank_reorder" if "k_rank_reorder" in names else "k_rank_cells"
-    head = ["k_predict_hash", *scan, "k_scatter", rank, "k_dense_sort", "k_gather", "k_neighbors_lambda"]
+    # small (latency-bound) steps rank per particle and split the neighbour
+    # walk over lanes; larger ones rank per cell
+    small = "k_rank_reorder" in names
+    rank = "k_rank_reorder" if small else "k_rank_cells"
+    walk = "k_neighbors_split" if small else "k_neighbors_lambda"
+    head = ["k_predict_hash", *scan, "k_scatter", rank, "k_dense_sort", "k_gather", walk]
     assert names[:len(head)] == head
     assert names.count("k_dp") == 4 and names.count("k_lambda") == 3
     assert b.launches == len(prof)
