@@ -647,8 +647,7 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.grid_omega = g(o.omega);
     sh.grid_apply = g(o.apply);
     sh.grid_xsph = g(o.xsph);
-    sh.grid_cells = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.cells),
-                                       std::max<uint32_t>(1, ctrl_.n_cell_tiles));
+    sh.grid_cells = std::max<uint32_t>(1, ctrl_.n_cell_tiles);  // a block per cell tile
     sh.small = (uint64_t)nt * tile <= kSmallStep ? 1u : 0u;
     sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), nt * (tile / 64));
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
