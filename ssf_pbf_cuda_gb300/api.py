@@ -684,10 +684,17 @@ def ssf_default_params(**overrides) -> dict:
     for k, _ in L.PbfSsfParams._fields_:
         v = getattr(s, k)
         d[k] = np.array(v[:], np.float32) if k in _SSF_ARRAYS else v
+    h0 = d["height"]
     for k, v in overrides.items():
         if k not in d:
             raise KeyError(k)
         d[k] = v
+    # both scales are proportional to the target height (main.cpp:445;
+    # pixels per unit at unit distance); follow an overridden height
+    if d["height"] != h0:
+        for k in ("blur_scale", "point_scale"):
+            if k not in overrides:
+                d[k] = float(np.float32(d[k]) * np.float32(d["height"]) / np.float32(h0))
     return d
 
 
