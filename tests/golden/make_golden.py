@@ -1,10 +1,10 @@
 """Generate golden fixtures from the reference's own CUDA step.
 
 Run on a machine with a GPU after `python oracle/ref_build.py` has prepared
-oracle/_ref/src (where the reference is mounted) — the binary itself is built
-here (ref_build.build), so it can run on the GPU machine:
+oracle/_ref/src (where the reference is mounted); the binary itself is built
+on the machine that runs it (ref_build.build):
 
-    python tests/golden/make_golden.py [out_dir]
+    python tests/golden/make_golden.py [out_dir]    (default: this directory)
 
 Each fixture holds the seeded input, the parameters, and the reference's
 outputs: num, sorted positions/velocities, sorted hash and index arrays,
@@ -186,4 +186,4 @@ def main(out_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))
