@@ -12,7 +12,7 @@ changes, which this recipe applies to a scratch copy under oracle/_ref/src
      in pbf_xsph.cu and pbf_vorticity_confinement.cu;
   4. GLM_FORCE_CUDA is not defined (GLM 0.9.7 rejects CUDA 13 with it).
 The copy is made where the reference is mounted (prepare); the build runs
-wherever nvcc is (the GPU machine builds its own aarch64 binary from the copy).
+wherever nvcc is (a machine of another architecture builds its own binary from the copy).
 Outputs go only to oracle/_ref/.  The reference's own build files are not used.
 """
 from __future__ import annotations
