@@ -641,7 +641,7 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
     auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), nt); };
     sh.grid = g(o.light);
-    sh.grid_nb = g(o.nb);
+    sh.grid_nb = nt;  // a block per tile: the walk's cost varies per tile, and fresh blocks balance it
     sh.grid_lambda = g(o.lambda);
     sh.grid_dp = g(o.dp);
     sh.grid_omega = g(o.omega);
