@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         carry = 0;
-        *a.dense = 0;  // the bucket queues of this step's k_rank_cells
+        *a.dense = 0;  // the bucket queues of this step's rank kernel
         *a.mid = 0;
     }
     __syncthreads();
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(StepArgs a)
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         carry = 0;
-        *a.dense = 0;  // the bucket queues of this step's k_rank_cells
+        *a.dense = 0;  // the bucket queues of this step's rank kernel
         *a.mid = 0;
     }
     __syncthreads();
@@ -711,7 +711,8 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     TILE_LOOP_END
 }
 
-// Buckets queued by k_rank_cells.  Medium ones (kMidMin+1 .. kDenseMin
+// Buckets queued by the rank kernels (k_rank_cells queues medium and dense
+// ones, k_rank_reorder dense ones).  Medium ones (kMidMin+1 .. kDenseMin
 // members) first, a warp each: members in lanes, each ranked by counting
 // over the others (broadcast by shuffle).  Dense ones (kDenseMin+1 ..
 // kStableLimit) then, a block each: the bucket entries (input index, alias
