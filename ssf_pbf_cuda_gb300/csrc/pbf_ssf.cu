@@ -221,7 +221,18 @@ __global__ void __launch_bounds__(256) k_ssf_raster(const SplatRec *__restrict__
     const uint32_t n = n_dev ? *n_dev : n_arg;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += warps) {
+    // Draw near particles first, so the early rejection finds nearer depths
+    // already in place: particle sets are often ordered along one axis
+    // (lattices, cell-sorted phases), so walk them in reverse when the last
+    // particle sits nearer the camera than the first.  Order changes no
+    // result: the depth test keeps the minimum.
+    bool reverse = false;
+    if (n > 1) {
+        const float z0 = __uint_as_float(rec[0].b.x), z1 = __uint_as_float(rec[n - 1].b.x);
+        reverse = z1 > z0;  // view space looks down -z: larger z is nearer
+    }
+    for (uint32_t p0 = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p0 < n; p0 += warps) {
+        const uint32_t p = reverse ? n - 1 - p0 : p0;
         const uint4 rb = rec[p].b;
         const uint32_t bw = rb.w & 0xffffu;
         if (bw == 0u) continue;
