@@ -558,39 +558,54 @@ def main():
     # ---------------- e2e through the C ABI with host buffers ----------------
     e2e = None
     if not args.no_e2e:
-        # Two batches of the same scenes on two streams, used alternately:
-        # step k's upload and compute are issued before step k-1's results
-        # are read back, so one batch's copies overlap the other's compute
-        # (every step still copies its inputs in and its results out).
+        # One batch; every step copies its inputs host -> device and its
+        # results device -> host (pinned host buffers).  The copies run on a
+        # copy stream through device staging buffers (two for the inputs), so
+        # step k+1's upload and step k-1's download overlap step k's compute;
+        # the compute stream runs pbf_batch_set_all from the staged inputs,
+        # the step and pbf_batch_get_all into the staged outputs.
         xh = torch.from_numpy(x0h).pin_memory()
         vh = torch.from_numpy(v0h).pin_memory()
-        xhp, vhp = xh.numpy(), vh.numpy()
-        batch2 = api.Batch(len(scs), n_total, cells, 30, device=local)
-        for sc, p, b in zip(scs, params, bnds):
-            batch2.add_scene(p, sc.n, sc.domain_end, b, sc.area, sc.x, sc.v)
-        batch2.set_tile(tile)
-        batch2.set_chunk(shape["chunk"])
-        lanes = []
-        for bb in (batch, batch2):
-            xo = torch.empty_like(xh).pin_memory()
-            vo = torch.empty_like(vh).pin_memory()
-            lanes.append((bb, torch.cuda.Stream(dev), xo.numpy(), vo.numpy()))
+        xo = torch.empty_like(xh).pin_memory()
+        vo = torch.empty_like(vh).pin_memory()
+        xin = [torch.empty(xh.shape, dtype=xh.dtype, device=dev) for _ in range(2)]
+        vin = [torch.empty(vh.shape, dtype=vh.dtype, device=dev) for _ in range(2)]
+        xout = torch.empty(xh.shape, dtype=xh.dtype, device=dev)
+        vout = torch.empty(vh.shape, dtype=vh.dtype, device=dev)
+        cs = torch.cuda.Stream(dev)
+        in_ready = [torch.cuda.Event(), torch.cuda.Event()]
+        out_ready, out_free = torch.cuda.Event(), torch.cuda.Event()
 
-        def issue(k):
-            bb, st, _, _ = lanes[k % 2]
-            bb.set_all(xhp, vhp, counts, st)
-            bb.step(ITERS, st)
+        def upload(k):
+            with torch.cuda.stream(cs):
+                xin[k % 2].copy_(xh, non_blocking=True)
+                vin[k % 2].copy_(vh, non_blocking=True)
+                in_ready[k % 2].record(cs)
 
-        def finish(k):
-            bb, st, xo, vo = lanes[k % 2]
-            bb.get_all(xo, vo, st)
+        def compute(k):
+            stream.wait_event(in_ready[k % 2])
+            batch.set_all(xin[k % 2], vin[k % 2], counts, stream)
+            batch.step(ITERS, stream)
+
+        def download():
+            stream.wait_event(out_free)  # the previous download has left the staging buffer
+            batch.get_all(xout, vout, stream)  # waits for the step (live counts), packs on the stream
+            out_ready.record(stream)
+            cs.wait_event(out_ready)
+            with torch.cuda.stream(cs):
+                xo.copy_(xout, non_blocking=True)
+                vo.copy_(vout, non_blocking=True)
+                out_free.record(cs)
 
         def e2e_run(n_steps):
-            issue(0)
+            upload(0)
+            compute(0)
             for k in range(1, n_steps):
-                issue(k)
-                finish(k - 1)
-            finish(n_steps - 1)
+                upload(k)
+                download()
+                compute(k)
+            download()
+            cs.synchronize()
 
         e2e_run(max(args.warmup, 2))
         barrier()
@@ -606,9 +621,10 @@ def main():
         e2e = {"value": job_particles * args.steps / dt, "unit": UNIT,
                "h2d_bytes_per_step": int(x0h.nbytes + v0h.nbytes), "d2h_bytes_per_step": int(x0h.nbytes + v0h.nbytes),
                "ms_per_step": dt / args.steps * 1e3,
-               "pipeline": "two batches on two streams, steps alternate; pbf_batch_set_all / step / get_all "
-                           "with pinned host buffers"}
-        del batch2, lanes
+               "pipeline": "one batch; host->device and device->host copies of pinned buffers on a copy "
+                           "stream through device staging, overlapping the neighbouring steps' compute; "
+                           "pbf_batch_set_all / step / get_all on the compute stream"}
+        del xin, vin, xout, vout
 
     # ---------------- plain: the same scenes one at a time ----------------
     plain = None
