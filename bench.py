@@ -46,6 +46,7 @@ ALG_STEP_P = 192 + 88 * ITERS + 160      # + XSPH and vorticity (configured phys
 ALG_STEP_C = 20 + 16 * ITERS + 24
 ALG_KERNEL = {  # per launch: (bytes per particle, bytes per cell)
     "k_dp": (52, 8), "k_lambda": (36, 8), "k_neighbors_lambda": (36, 8),
+    "k_neighbors_split": (36, 8),
     "k_predict_hash": (52, 4), "k_xsph": (48, 8), "k_vort_omega": (48, 8), "k_vort_apply": (64, 8),
 }
 

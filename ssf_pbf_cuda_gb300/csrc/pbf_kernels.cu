@@ -61,6 +61,9 @@ __device__ __forceinline__ float dist2_exact(float4 a, float4 b)
 
 // Kernel value and gradient for a listed pair at current positions:
 // memorizeKernelPair, src/pbf/solver/cuda/pbf_kernel_memorization.cu:14-56.
+// Every product and sum is explicitly rounded (no contraction left to the
+// compiler), here and in the sums below, so that the one-lane passes and the
+// split passes of small steps give the same bits.
 struct PairK {
     float W;
     float gx, gy, gz;
@@ -69,25 +72,53 @@ struct PairK {
 __device__ __forceinline__ PairK pair_kernel(float4 xi, float4 xj, float inv_h, float alpha, float beta)
 {
     PairK o;
-    const float d0 = xi.x - xj.x, d1 = xi.y - xj.y, d2 = xi.z - xj.z;
-    const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
+    const float d0 = __fsub_rn(xi.x, xj.x), d1 = __fsub_rn(xi.y, xj.y), d2 = __fsub_rn(xi.z, xj.z);
+    const float r2 = __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
     const float inv_r = rsqrtf(r2);
-    const float q2 = r2 * inv_h * inv_h;
+    const float q2 = __fmul_rn(__fmul_rn(r2, inv_h), inv_h);
     o.W = 0.f;
     if (q2 <= 1.f) {
-        const float t = 1.f - q2;
-        o.W = alpha * t * t * t;
+        const float t = __fsub_rn(1.f, q2);
+        o.W = __fmul_rn(__fmul_rn(__fmul_rn(alpha, t), t), t);
     }
-    const float r = r2 * inv_r;
-    const float u = fmaf(-r, inv_h, 1.f);
-    const float kd = (inv_h <= inv_r) ? beta * u * u : 0.f;
+    const float r = __fmul_rn(r2, inv_r);
+    const float u = __fmaf_rn(-r, inv_h, 1.f);
+    const float kd = (inv_h <= inv_r) ? __fmul_rn(__fmul_rn(beta, u), u) : 0.f;
     // grad W = 0 for the pair with itself (r2 = 0, where kd and inv_r are not finite)
-    const float s = (r2 > 0.f) ? kd * inv_r : 0.f;
-    o.gx = s * d0;
-    o.gy = s * d1;
-    o.gz = s * d2;
+    const float s = (r2 > 0.f) ? __fmul_rn(kd, inv_r) : 0.f;
+    o.gx = __fmul_rn(s, d0);
+    o.gy = __fmul_rn(s, d1);
+    o.gz = __fmul_rn(s, d2);
     return o;
 }
+
+// |grad W|^2 of a pair, in the order calcScalingFactor sums it (z, y, x).
+__device__ __forceinline__ float grad2(const PairK &p)
+{
+    return __fmaf_rn(p.gz, p.gz, __fmaf_rn(p.gy, p.gy, __fmul_rn(p.gx, p.gx)));
+}
+
+// The sums of calcScalingFactorCUDA (pbf_constraint.cu:168-209) over a
+// particle's list, added in list order.
+struct LamSum {
+    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+    __device__ __forceinline__ void add(float W, float gx, float gy, float gz, float k2)
+    {
+        ks = __fadd_rn(ks, W);
+        g0 = __fadd_rn(g0, gx);
+        g1 = __fadd_rn(g1, gy);
+        g2 = __fadd_rn(g2, gz);
+        kg2 = __fadd_rn(kg2, k2);
+    }
+    __device__ __forceinline__ void add(const PairK &p) { add(p.W, p.gx, p.gy, p.gz, grad2(p)); }
+    // lambda = C / (m^2 / rho0^2 |grad C|^2 + eps)
+    __device__ __forceinline__ float lambda(const SceneDesc &d) const
+    {
+        const float C = __fmaf_rn(__fmul_rn(ks, d.m), d.inv_rho0, -1.f);
+        const float K = __fmaf_rn(g0, g0, __fmaf_rn(g2, g2, __fmaf_rn(g1, g1, kg2)));
+        return __fdiv_rn(C, __fmaf_rn(d.m2rho2, K, d.relax));
+    }
+};
 
 // WspikyDerivative, src/pbf/kernel/cuda/detail/pbf_kernel.inl:48-63.
 __device__ __forceinline__ float wspiky_d(float r, float kinv_h)
@@ -914,22 +945,15 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     a.nnb[i] = (uint8_t)cnt;
     // phase 2: lambda over the list just written (L2-resident; plain loads,
     // the read-only path may not see this kernel's own stores)
-    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
+    LamSum ls;
     const uint32_t *rd = nl;
 #pragma unroll 4
     for (uint32_t k = 0; k < cnt; ++k) {
         const uint32_t q = *rd;
         rd += stride;
-        const PairK pk = pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta);
-        ks += pk.W;
-        g0 += pk.gx;
-        g1 += pk.gy;
-        g2 += pk.gz;
-        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+        ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
     }
-    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
-    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-    a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
+    a.lam[i] = ls.lambda(d);
     TILE_LOOP_END
 }
 
@@ -943,6 +967,51 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 // bit).  Scenes with more than kSplitCap list slots walk in one lane.
 constexpr uint32_t kSplit = 4;
 constexpr uint32_t kSplitCap = 64;
+
+// Small steps: a sum over one particle's list split over the particle's
+// kSplit lanes.  Lane sub evaluates slots sub, sub + kSplit, ...; each
+// round's terms reach every lane of the group by shuffles and are added in
+// list order, so every lane ends with the one-lane sums, bit for bit.  List
+// indices are requested two rounds ahead and positions one round ahead (a
+// slot past the list reads index 0, a valid slot, and adds nothing).  RO:
+// the list is read through the read-only path (it was not written by this
+// kernel).
+template <bool RO>
+__device__ __forceinline__ uint32_t split_index(const uint32_t *nl, uint64_t stride, uint32_t nn, uint32_t k)
+{
+    if (k >= nn) return 0u;
+    const uint32_t *p = nl + (uint64_t)k * stride;
+    return RO ? __ldg(p) : *p;
+}
+
+template <bool RO>
+__device__ __forceinline__ LamSum lam_sum_split(const uint32_t *nl, uint64_t stride, uint32_t nn,
+                                                const float4 *__restrict__ xc, float4 xp, const SceneDesc &d,
+                                                uint32_t sub, uint32_t gmask)
+{
+    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    LamSum ls;
+    float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub));
+    uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit);
+    for (uint32_t k0 = 0; k0 < nn; k0 += kSplit) {
+        const float4 x1 = __ldg(xc + q1);
+        q1 = split_index<RO>(nl, stride, nn, k0 + 2 * kSplit + sub);
+        PairK pk{0.f, 0.f, 0.f, 0.f};
+        if (k0 + sub < nn) pk = pair_kernel(xp, x0, inv_h, alpha, beta);
+        const float k2 = grad2(pk);
+#pragma unroll
+        for (uint32_t j = 0; j < kSplit; ++j) {
+            const float W = __shfl_sync(gmask, pk.W, j, kSplit);
+            const float gx = __shfl_sync(gmask, pk.gx, j, kSplit);
+            const float gy = __shfl_sync(gmask, pk.gy, j, kSplit);
+            const float gz = __shfl_sync(gmask, pk.gz, j, kSplit);
+            const float kk = __shfl_sync(gmask, k2, j, kSplit);
+            if (k0 + j < nn) ls.add(W, gx, gy, gz, kk);
+        }
+        x0 = x1;
+    }
+    return ls;
+}
 __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t tile)
 {
     const uint32_t per_block = blockDim.x / kSplit;  // particles per block
@@ -1018,26 +1087,13 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
             for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) nl[(uint64_t)(pre + t) * stride] = buf[t];
         }
         const uint32_t nn = total < cap ? total : cap;
-        __syncwarp(gmask);  // the list entries of the group are visible to its first lane
-        if (sub != 0) continue;
-        a.nnb[i] = (uint8_t)nn;
-        const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-        float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-        const uint32_t *rd = nl;
-#pragma unroll 4
-        for (uint32_t k = 0; k < nn; ++k) {
-            const uint32_t q = *rd;
-            rd += stride;
-            const PairK pk = pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta);
-            ks += pk.W;
-            g0 += pk.gx;
-            g1 += pk.gy;
-            g2 += pk.gz;
-            kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
+        __syncwarp(gmask);  // the list entries of the group are visible to all its lanes
+        // lambda of iteration 0 over the list, split over the group's lanes
+        const LamSum ls = lam_sum_split<false>(nl, stride, nn, xa, xp, d, sub, gmask);
+        if (sub == 0) {
+            a.nnb[i] = (uint8_t)nn;
+            a.lam[i] = ls.lambda(d);
         }
-        const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
-        const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
-        a.lam[i] = C / fmaf(d.m2rho2, K, d.relax);
     }
 }
 
@@ -1056,22 +1112,14 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const uint32_t i = d.p_off + local;
     const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
     const float4 xp = xc[i];
-    float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
-        const PairK pk = pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta);
-        ks += pk.W;
-        g0 += pk.gx;
-        g1 += pk.gy;
-        g2 += pk.gz;
-        kg2 += fmaf(pk.gz, pk.gz, fmaf(pk.gy, pk.gy, pk.gx * pk.gx));
-    });
-    const float C = fmaf(ks * d.m, d.inv_rho0, -1.f);
-    const float K = fmaf(g0, g0, fmaf(g2, g2, fmaf(g1, g1, kg2)));
+    LamSum ls;
+    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i],
+                      [&](uint32_t q) { ls.add(pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta)); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
     // delta-p pass gathers next (neighbours here use only .xyz); small,
     // latency-bound steps keep it in its own array, as the store into the
     // gathered array slows this pass's neighbour reads there
-    const float lam = C / fmaf(d.m2rho2, K, d.relax);
+    const float lam = ls.lambda(d);
     if (LAMW)
         reinterpret_cast<float *>(xc + i)[3] = lam;
     else
@@ -1082,42 +1130,83 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
 // s_corr forms, selected once per tile (a tile belongs to one scene).
 enum ScorrForm { kScorrReference, kScorrTextbook, kScorrOff, kScorrTextbook4 };
 
+struct ScorrConst {
+    float sci;  // max(-lambda_i, 0), the reference form's own share
+    float inv_k, inv_wdq, sk;
+    int sn;
+};
+
+// -(lambda_i + lambda_j + s_corr) for a pair (the coefficient of grad W in
+// calcPositionUpdateCUDA, pbf_position_update.cu:131-188), with s_corr's last
+// product fused into the sum.
+template <int FORM>
+__device__ __forceinline__ float dp_coef(float li, float lj, float W, const ScorrConst &c)
+{
+    const float ll = __fadd_rn(li, lj);
+    if (FORM == kScorrReference) {
+        const float kr2 = __fmul_rn(W, W);
+        const float tc = __fmul_rn(__fmul_rn(10.f, __fmul_rn(kr2, kr2)), c.inv_k);
+        return -__fmaf_rn(__fadd_rn(c.sci, (lj < 0.f) ? -lj : 0.f), tc, ll);
+    } else if (FORM == kScorrTextbook4) {  // the loop below for n = 4, same products in the same order
+        const float ratio = __fmul_rn(W, c.inv_wdq);
+        return -__fmaf_rn(c.sk, __fmul_rn(__fmul_rn(__fmul_rn(ratio, ratio), ratio), ratio), ll);
+    } else if (FORM == kScorrTextbook) {
+        const float ratio = __fmul_rn(W, c.inv_wdq);
+        float pw = 1.f;
+        for (int e = 0; e < c.sn; ++e) pw = __fmul_rn(pw, ratio);
+        return -__fmaf_rn(c.sk, pw, ll);
+    }
+    return -ll;
+}
+
+__device__ __forceinline__ ScorrConst scorr_const(const SceneDesc &d, float li)
+{
+    ScorrConst c;
+    c.sci = (li < 0.f) ? -li : 0.f;
+    c.inv_k = d.inv_k;
+    c.inv_wdq = d.inv_wdq;
+    c.sk = d.scorr_k;
+    c.sn = d.scorr_n;
+    return c;
+}
+
 // Sum over the list of -(lambda_i + lambda_j + s_corr) grad W (the body of
-// calcPositionUpdateCUDA, pbf_position_update.cu:131-188).
+// calcPositionUpdateCUDA, pbf_position_update.cu:131-188), in list order.
 template <int kChunk, int FORM, bool LAMW>
 __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, const float4 *__restrict__ xc,
                                          uint32_t i, float4 xp, float li)
 {
     const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
-    const float sci = (li < 0.f) ? -li : 0.f;
-    const float inv_k = d.inv_k, inv_wdq = d.inv_wdq, sk = d.scorr_k;
-    const int sn = d.scorr_n;
+    const ScorrConst sc = scorr_const(d, li);
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
         const float4 xq = __ldg(xc + q);
         const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
         const float lj = LAMW ? xq.w : __ldg(lam + q);  // LAMW: lambda in .w of the positions
-        float corr = 0.f;
-        if (FORM == kScorrReference) {
-            const float kr2 = pk.W * pk.W;
-            const float tc = 10.f * (kr2 * kr2) * inv_k;
-            corr = (sci + ((lj < 0.f) ? -lj : 0.f)) * tc;
-        } else if (FORM == kScorrTextbook4) {  // the loop below for n = 4, same products in the same order
-            const float ratio = pk.W * inv_wdq;
-            corr = sk * (((ratio * ratio) * ratio) * ratio);
-        } else if (FORM == kScorrTextbook) {
-            const float ratio = pk.W * inv_wdq;
-            float pw = 1.f;
-            for (int e = 0; e < sn; ++e) pw *= ratio;
-            corr = sk * pw;
-        }
-        const float cc = -(li + lj + corr);
-        s0 += cc * pk.gx;
-        s1 += cc * pk.gy;
-        s2 += cc * pk.gz;
+        const float cc = dp_coef<FORM>(li, lj, pk.W, sc);
+        s0 = __fmaf_rn(cc, pk.gx, s0);
+        s1 = __fmaf_rn(cc, pk.gy, s1);
+        s2 = __fmaf_rn(cc, pk.gz, s2);
     });
     return make_float3(s0, s1, s2);
+}
+
+// A particle's delta-p from the list sum: scale, boundary response, x += dp
+// into the second buffer, and on the last iteration the velocity and id.
+__device__ __forceinline__ void dp_finish(const StepArgs &a, const SceneDesc &d, uint32_t s, uint32_t i, float4 xp,
+                                          float3 sum, float4 *__restrict__ xo, float4 *__restrict__ vo, int last)
+{
+    float3 dp = make_float3(sum.x * d.m * d.inv_rho0, sum.y * d.m * d.inv_rho0, sum.z * d.m * d.inv_rho0);
+    const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
+    if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
+    const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
+    xo[i] = xn;
+    if (last) {
+        const float4 xo_ = a.xold[i];
+        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+        a.id[i] = a.id_tmp[i];  // ids follow the particles into sorted order
+    }
 }
 
 // delta-p with s_corr (calcPositionUpdateCUDA cached, pbf_position_update.cu:131-188),
@@ -1148,16 +1237,7 @@ __global__ void __launch_bounds__(512, 2) k_dp(StepArgs a, const float4 *__restr
         sum = dp_sum<kChunk, kScorrTextbook, LAMW>(a, d, xc, i, xp, li);
     else
         sum = dp_sum<kChunk, kScorrOff, LAMW>(a, d, xc, i, xp, li);
-    float3 dp = make_float3(sum.x * d.m * d.inv_rho0, sum.y * d.m * d.inv_rho0, sum.z * d.m * d.inv_rho0);
-    const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
-    if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
-    const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
-    xo[i] = xn;
-    if (last) {
-        const float4 xo_ = a.xold[i];
-        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
-        a.id[i] = a.id_tmp[i];  // ids follow the particles into sorted order
-    }
+    dp_finish(a, d, s, i, xp, sum, xo, vo, last);
     TILE_LOOP_END
 }
 
