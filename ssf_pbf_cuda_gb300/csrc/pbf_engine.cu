@@ -653,6 +653,15 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan
+    sh.scan_rounds = 0;
+    if (sh.scan_grid == 0) {
+        const uint32_t r = (ctrl_.n_cells + 1023u) / 1024u;
+        for (uint32_t p = 1; p <= 16; p <<= 1)
+            if (r <= p) {
+                sh.scan_rounds = p;
+                break;
+            }
+    }
     return sh;
 }
 

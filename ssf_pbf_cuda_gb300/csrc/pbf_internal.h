@@ -94,16 +94,18 @@ struct LaunchShape {
     uint32_t tile;        // particles per tile = threads per block
     uint32_t grid;        // persistent grid (blocks) for the light tile kernels
     uint32_t scan_grid;   // grid for the scan kernels; 0 = the one-block scan
+    uint32_t scan_rounds; // one-block scan: rounds of 1024 cells held in registers (1..16), 0 = looped
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
-    uint32_t grid_cells;  // persistent grid of k_rank_cells (blocks of kCellTile threads)
+    uint32_t grid_cells;  // grid of k_rank_cells: a block of kCellTile threads per cell tile
     uint32_t small;       // latency-bound step (at most kSmallStep particle slots): split
                           // neighbour walk, per-particle rank, lambda kept in its own array
     uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 64 particles each)
     bool operator==(const LaunchShape &o) const
     {
-        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && chunk == o.chunk &&
+        return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && scan_rounds == o.scan_rounds &&
+               chunk == o.chunk &&
                grid_cells == o.grid_cells && small == o.small && grid_split == o.grid_split &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;

@@ -506,6 +506,55 @@ __global__ void __launch_bounds__(1024) k_scan_spine(StepArgs a)
     if (threadIdx.x == 0) a.offsets[n] = carry;
 }
 
+// The whole scan in one block for tables of at most 1024 * R cells, R
+// rounds of 1024 held in registers: every round's counts are requested at
+// once (coalesced), the rounds' warp scans run side by side, one warp turns
+// the rounds' warp totals into offsets (carrying across rounds in order),
+// and the offsets are written coalesced.  Two barriers in all.
+template <uint32_t R>
+__global__ void __launch_bounds__(1024) k_scan_single_reg(StepArgs a)
+{
+    __shared__ uint32_t ws[R][32];
+    const uint32_t n = a.ctrl->n_cells;
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    if (t == 0) {
+        *a.dense = 0;  // the bucket queues of this step's rank kernel
+        *a.mid = 0;
+    }
+    uint32_t v[R], inc[R];
+#pragma unroll
+    for (uint32_t k = 0; k < R; ++k) {
+        const uint32_t idx = k * 1024u + t;
+        v[k] = idx < n ? a.count[idx] : 0u;
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < R; ++k) {
+        inc[k] = warp_incl_scan(v[k]);
+        if (lane == 31) ws[k][warp] = inc[k];
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive prefix of every (round, warp) total, rounds in order
+        uint32_t carry = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < R; ++k) {
+            const uint32_t wv = ws[k][lane];
+            const uint32_t wi = warp_incl_scan(wv);
+            ws[k][lane] = carry + wi - wv;
+            carry += __shfl_sync(0xffffffffu, wi, 31);
+        }
+        if (lane == 0) a.offsets[n] = carry;
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < R; ++k) {
+        const uint32_t idx = k * 1024u + t;
+        if (idx < n) {
+            a.offsets[idx] = ws[k][warp] + inc[k] - v[k];
+            a.count[idx] = 0u;  // ready for the next step's histogram
+        }
+    }
+}
+
 // The whole scan in one block, for tables of at most kSingleScanMax cells
 // (small scenes: one launch instead of three).
 __global__ void __launch_bounds__(1024) k_scan_single(StepArgs a)
@@ -1598,7 +1647,14 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     k_predict_hash<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_predict_hash");
     if (sh.scan_grid == 0) {  // small table: one block
-        k_scan_single<<<1, 1024, 0, st>>>(a);
+        switch (sh.scan_rounds) {  // rounds of 1024 cells held in registers
+        case 1: k_scan_single_reg<1><<<1, 1024, 0, st>>>(a); break;
+        case 2: k_scan_single_reg<2><<<1, 1024, 0, st>>>(a); break;
+        case 4: k_scan_single_reg<4><<<1, 1024, 0, st>>>(a); break;
+        case 8: k_scan_single_reg<8><<<1, 1024, 0, st>>>(a); break;
+        case 16: k_scan_single_reg<16><<<1, 1024, 0, st>>>(a); break;
+        default: k_scan_single<<<1, 1024, 0, st>>>(a); break;
+        }
         PBF_LAUNCHED("k_scan_single");
     } else {
         k_scan_reduce<<<sh.scan_grid, 256, 0, st>>>(a);
