@@ -649,7 +649,7 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.grid_xsph = g(o.xsph);
     sh.grid_cells = std::max<uint32_t>(1, ctrl_.n_cell_tiles);  // a block per cell tile
     sh.small = (uint64_t)nt * tile <= kSmallStep ? 1u : 0u;
-    sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), nt * (tile / 64));
+    sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), nt * (tile / (256 / kSplit)));
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan

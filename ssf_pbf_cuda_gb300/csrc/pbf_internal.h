@@ -101,7 +101,7 @@ struct LaunchShape {
     uint32_t grid_cells;  // grid of k_rank_cells: a block of kCellTile threads per cell tile
     uint32_t small;       // latency-bound step (at most kSmallStep particle slots): split
                           // neighbour walk, per-particle rank, lambda kept in its own array
-    uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 64 particles each)
+    uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 256 / kSplit particles each)
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && scan_rounds == o.scan_rounds &&
@@ -160,6 +160,7 @@ constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;
 constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells per scan tile
 constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
+constexpr uint32_t kSplit = 4;  // small steps: lanes per particle in the split neighbour walk (blocks of 256)
 constexpr uint32_t kCellTile = 256;         // cells per cell tile = threads per k_rank_cells block
 constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)
 constexpr uint32_t kSmallStep = 131072;     // particle slots up to which a step is latency bound

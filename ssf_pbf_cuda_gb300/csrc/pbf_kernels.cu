@@ -1011,11 +1011,20 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 // private buffer of at most cap entries.  A prefix over the group's counts
 // then places every lane's entries after those of the rows before it, so the
 // list holds the first cap accepted candidates in the reference's walk
-// order, as k_neighbors_lambda's.  The particle's first lane then sums the
-// iteration-0 lambda over the list in list order (the same sum, bit for
+// order, as k_neighbors_lambda's.  The group then sums the iteration-0
+// lambda over the list in list order (lam_sum_split: the same sum, bit for
 // bit).  Scenes with more than kSplitCap list slots walk in one lane.
-constexpr uint32_t kSplit = 4;
 constexpr uint32_t kSplitCap = 64;
+static_assert(kSplit == 4 || kSplit == 8, "a particle's lanes share one aligned group of a warp");
+
+// The (dz, dy) rows [rr0, rr1) of a particle's lane sub: rows shared evenly,
+// the first lane taking the one left over.
+__device__ __forceinline__ void split_rows(uint32_t sub, int &rr0, int &rr1)
+{
+    constexpr int per = 9 / (int)kSplit, extra = 9 - per * (int)kSplit;
+    rr0 = sub == 0 ? 0 : extra + per * (int)sub;
+    rr1 = extra + per * ((int)sub + 1);
+}
 
 // Small steps: a sum over one particle's list split over the particle's
 // kSplit lanes.  Lane sub evaluates slots sub, sub + kSplit, ...; each
@@ -1066,7 +1075,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
     const uint32_t per_block = blockDim.x / kSplit;  // particles per block
     const uint32_t parts = tile / per_block;         // blocks per tile
     const uint32_t lane = threadIdx.x & 31u, sub = threadIdx.x % kSplit;
-    const uint32_t gmask = 0xFu << (lane & ~3u);    // the particle's kSplit lanes
+    const uint32_t gmask = ((1u << kSplit) - 1u) << (lane & ~(kSplit - 1u));  // the particle's lanes
     const uint32_t n_work = a.ctrl->n_tiles * parts;
     for (uint32_t u = blockIdx.x; u < n_work; u += gridDim.x) {
         const uint32_t t_ = u / parts;
@@ -1085,11 +1094,11 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         uint32_t *nl = a.nbr + i;
         const float4 *__restrict__ xa = a.xa;
         const float4 *__restrict__ wx = a.wx;
-        // rows {0,1,2} {3,4} {5,6} {7,8}; one lane takes all nine when the
-        // list does not fit the private buffer
+        // rows shared over the lanes (split_rows); one lane takes all nine
+        // when the list does not fit the private buffer
         const bool one = cap > kSplitCap;
-        const int rr0 = one ? (sub == 0 ? 0 : 9) : (sub == 0 ? 0 : 1 + 2 * (int)sub);
-        const int rr1 = one ? (sub == 0 ? 9 : 9) : 3 + 2 * (int)sub;
+        int rr0 = sub == 0 ? 0 : 9, rr1 = 9;
+        if (!one) split_rows(sub, rr0, rr1);
         uint32_t buf[kSplitCap];
         uint32_t cnt = 0;
         if (one && sub == 0) {  // write straight into the list

@@ -92,3 +92,24 @@ def test_long_run_statistics_match_fp64_oracle(oracle, gpu):
     assert abs(ke_g - ke_o) <= max(0.01 * ke_o, 2.0 * abs(ke_32 - ke_o))
     de_g, de_o, de_32 = mean_density_error(xg), mean_density_error(xo), mean_density_error(x32)
     assert abs(de_g - de_o) <= max(0.01 * de_o + 1e-4, 2.0 * abs(de_32 - de_o))
+
+
+@pytest.mark.parametrize("grid", [(4, 4, 4), (16, 16, 8), (16, 16, 16), (32, 16, 16), (32, 32, 16),
+                                  (32, 32, 32), (64, 32, 32)])
+def test_one_block_scan_every_table_size(oracle, gpu, grid):
+    """Tables of up to 65,536 cells are scanned by one block: up to 16,384
+    cells with 1, 2, 4, 8 or 16 rounds of 1,024 held in registers, above
+    that round by round.  Cell ranges and the permutation equal the oracle's
+    for a table of each size (particles spread over it, some cells empty)."""
+    g = np.random.default_rng(sum(grid))
+    cw = 0.1
+    n = 3 * int(np.prod(grid)) // 4
+    x = (g.random((n, 3)) * np.asarray(grid) * cw).astype(np.float32)
+    d = gpu_sort_only(x, grid, cw)
+    keys, perm, off = oracle.hash_sort(x, cw, grid)
+    C = int(np.prod(grid))
+    assert np.array_equal(d["perm"], perm)
+    ne = off[1:C + 1] > off[:C]
+    assert 0 < ne.sum() < C
+    assert np.array_equal(d["cell_start"] != 0xFFFFFFFF, ne)
+    assert np.array_equal(d["cell_start"][ne], off[:C][ne]) and np.array_equal(d["cell_end"][ne], off[1:C + 1][ne])
