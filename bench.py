@@ -315,6 +315,34 @@ def ssf_alg_bytes(w: int, h: int, n: int, blur_passes: int) -> int:
     return (4 + 8 * blur_passes + 20 + 40) * w * h + 12 * n
 
 
+def run_dam32k(api, torch, dev, stream, warmup: int, reps: int) -> dict:
+    """The plain 32,768-particle dam break: `reps` plain steps through
+    pbf_one_step, each from the seeded initial state, timed with CUDA events
+    on the launching stream."""
+    from ssf_pbf_cuda_gb300 import scenes
+    sc = scenes.config1()
+    p = scene_params(sc)
+    part = api.PbfParticle(p, sc.n, sc.domain_end, device=dev.index)
+    b = api.Boundary(points_on_planes=sc.planes[0], normals_on_planes=sc.planes[1])
+    xd = torch.from_numpy(sc.x).to(dev)
+    vd = torch.from_numpy(sc.v).to(dev)
+    for _ in range(warmup):
+        part.set_particles(xd, vd, stream)
+        api.one_step(part, b, sc.area, ITERS, stream)
+    torch.cuda.synchronize()
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    for _ in range(reps):
+        part.set_particles(xd, vd, stream)
+        api.one_step(part, b, sc.area, ITERS, stream)
+    c1.record(stream)
+    torch.cuda.synchronize()
+    cms = c0.elapsed_time(c1) / reps
+    return {"value": sc.n / (cms / 1e3), "unit": UNIT, "ms_per_step": cms, "launches_per_step": part.launches,
+            "workload": f"plain dam break: 32,768 particles (32x32x32), 4 x 2 x 2 m box, {reps} steps, "
+                        "each from the seeded initial state; launch / latency bound (L2-resident)"}
+
+
 def run_ssf_bench(api, torch, device: int, with_cpu: bool, frames: int = 200) -> dict:
     """Headless screen-space fluid frames (depth splat, blur x3, normals,
     shading), timed with CUDA events on the launching stream: the reference's
@@ -429,6 +457,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ssf", action="store_true", help="skip the screen-space fluid frame timing")
+    ap.add_argument("--dam32k-only", action="store_true",
+                    help="time only the plain 32,768-particle dam break (--warmup, then --steps steps)")
     ap.add_argument("--ssf-only", action="store_true",
                     help="time only the screen-space fluid frames and print their JSON object")
     ap.add_argument("--tile", type=int, default=0, help="0 = autotune")
@@ -468,6 +498,11 @@ def main():
 
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
+    if args.dam32k_only:
+        if rank == 0:
+            print(json.dumps({"plain_dam_32k": run_dam32k(api, torch, dev, stream, args.warmup, args.steps)}),
+                  flush=True)
+        return
 
     def barrier():
         if dist is not None:
@@ -706,29 +741,7 @@ def main():
     # ---------------- config 1: the plain 32,768-particle dam break ----------------
     small = None
     if not args.no_plain and rank == 0:
-        from ssf_pbf_cuda_gb300 import scenes
-        sc = scenes.config1()
-        p = scene_params(sc)
-        part = api.PbfParticle(p, sc.n, sc.domain_end, device=local)
-        b = api.Boundary(points_on_planes=sc.planes[0], normals_on_planes=sc.planes[1])
-        xd = torch.from_numpy(sc.x).to(dev)
-        vd = torch.from_numpy(sc.v).to(dev)
-        for _ in range(args.warmup):
-            part.set_particles(xd, vd, stream)
-            api.one_step(part, b, sc.area, ITERS, stream)
-        torch.cuda.synchronize()
-        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 100
-        c0.record(stream)
-        for _ in range(reps):
-            part.set_particles(xd, vd, stream)
-            api.one_step(part, b, sc.area, ITERS, stream)
-        c1.record(stream)
-        torch.cuda.synchronize()
-        cms = c0.elapsed_time(c1) / reps
-        small = {"value": sc.n / (cms / 1e3), "unit": UNIT, "ms_per_step": cms,
-                 "workload": "plain dam break: 32,768 particles (32x32x32), 4 x 2 x 2 m box, 100 steps, "
-                             "each from the seeded initial state; launch / latency bound (L2-resident)"}
+        small = run_dam32k(api, torch, dev, stream, args.warmup, 100)
 
     # ---------------- serving: Poisson arrivals, continuous batching ----------------
     serving = None

@@ -654,13 +654,9 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan
     sh.scan_rounds = 0;
-    if (sh.scan_grid == 0) {
-        const uint32_t r = (ctrl_.n_cells + 1023u) / 1024u;
-        for (uint32_t p = 1; p <= 16; p <<= 1)
-            if (r <= p) {
-                sh.scan_rounds = p;
-                break;
-            }
+    if (sh.scan_grid == 0) {  // the table's rounds of 1024 cells, if they fit in registers
+        const uint32_t r = std::max<uint32_t>(1, (ctrl_.n_cells + 1023u) / 1024u);
+        if (r <= 16) sh.scan_rounds = r;
     }
     return sh;
 }

@@ -1657,11 +1657,13 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     PBF_LAUNCHED("k_predict_hash");
     if (sh.scan_grid == 0) {  // small table: one block
         switch (sh.scan_rounds) {  // rounds of 1024 cells held in registers
-        case 1: k_scan_single_reg<1><<<1, 1024, 0, st>>>(a); break;
-        case 2: k_scan_single_reg<2><<<1, 1024, 0, st>>>(a); break;
-        case 4: k_scan_single_reg<4><<<1, 1024, 0, st>>>(a); break;
-        case 8: k_scan_single_reg<8><<<1, 1024, 0, st>>>(a); break;
-        case 16: k_scan_single_reg<16><<<1, 1024, 0, st>>>(a); break;
+#define PBF_SCAN_ROUNDS(r) \
+    case r: k_scan_single_reg<r><<<1, 1024, 0, st>>>(a); break;
+        PBF_SCAN_ROUNDS(1) PBF_SCAN_ROUNDS(2) PBF_SCAN_ROUNDS(3) PBF_SCAN_ROUNDS(4)
+        PBF_SCAN_ROUNDS(5) PBF_SCAN_ROUNDS(6) PBF_SCAN_ROUNDS(7) PBF_SCAN_ROUNDS(8)
+        PBF_SCAN_ROUNDS(9) PBF_SCAN_ROUNDS(10) PBF_SCAN_ROUNDS(11) PBF_SCAN_ROUNDS(12)
+        PBF_SCAN_ROUNDS(13) PBF_SCAN_ROUNDS(14) PBF_SCAN_ROUNDS(15) PBF_SCAN_ROUNDS(16)
+#undef PBF_SCAN_ROUNDS
         default: k_scan_single<<<1, 1024, 0, st>>>(a); break;
         }
         PBF_LAUNCHED("k_scan_single");
