@@ -653,6 +653,10 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
     sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan
+    {  // the block's lists in shared memory when they fit
+        const uint64_t b = (uint64_t)tile * (max_pair_ - 1u) * 4u;
+        sh.nb_smem = b <= kNbSmemMax ? (uint32_t)b : 0u;
+    }
     sh.scan_rounds = 0;
     if (sh.scan_grid == 0) {  // the table's rounds of 1024 cells, if they fit in registers
         const uint32_t r = std::max<uint32_t>(1, (ctrl_.n_cells + 1023u) / 1024u);

@@ -102,11 +102,12 @@ struct LaunchShape {
     uint32_t small;       // latency-bound step (at most kSmallStep particle slots): split
                           // neighbour walk, per-particle rank, lambda kept in its own array
     uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 256 / kSplit particles each)
+    uint32_t nb_smem;     // k_neighbors_lambda: bytes of shared memory for the block's lists (0 = stored directly)
     bool operator==(const LaunchShape &o) const
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && scan_rounds == o.scan_rounds &&
                chunk == o.chunk &&
-               grid_cells == o.grid_cells && small == o.small && grid_split == o.grid_split &&
+               grid_cells == o.grid_cells && small == o.small && grid_split == o.grid_split && nb_smem == o.nb_smem &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
@@ -160,6 +161,7 @@ constexpr uint32_t kScanItemsPerWarp = 512;   // 32 lanes x 16
 constexpr uint32_t kScanWarps = 8;
 constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells per scan tile
 constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
+constexpr uint32_t kNbSmemMax = 96 * 1024;  // shared-memory budget for a k_neighbors_lambda block's lists
 constexpr uint32_t kSplit = 4;  // small steps: lanes per particle in the split neighbour walk (blocks of 256)
 constexpr uint32_t kCellTile = 256;         // cells per cell tile = threads per k_rank_cells block
 constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)

@@ -15,6 +15,10 @@
 // acceptance) uses explicitly rounded intrinsics so that it is bit-exact
 // against the CPU oracle.  Floating-point solver math follows the reference's
 // operation order but uses rsqrtf (as the reference does).
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "pbf_internal.h"
 #include "pbf103.h"
 
@@ -949,8 +953,15 @@ __global__ void __launch_bounds__(512) k_gather(StepArgs a)
 // (calcScalingFactorCUDA cached, pbf_constraint.cu:168-209): at iteration 0
 // the working positions are the sorted predicted positions, so the pair
 // terms can be summed while the list is built.
+// SMEM: the accepted indices are collected in shared memory (slot-major per
+// block, conflict-free) and written to the list by the lambda loop that
+// reads them back, so every list store of a warp is coalesced (the lanes'
+// slot k at consecutive particles) instead of one scattered 4-byte store per
+// accepted candidate.
+template <bool SMEM>
 __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 {
+    extern __shared__ uint32_t s_list[];  // SMEM: [slot][threadIdx.x]
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
     const uint32_t base = a.offsets[d.c_off];
@@ -972,7 +983,8 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // tested in order, so the first `cap` accepted ones are the reference's.
     constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
-    uint32_t *slot = nl;
+    uint32_t *slot = SMEM ? s_list + threadIdx.x : nl;
+    const uint32_t slot_step = SMEM ? blockDim.x : (uint32_t)stride;
     walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
                        [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
@@ -984,7 +996,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
                     *slot = __float_as_uint(c[k].w);
-                    slot += stride;
+                    slot += slot_step;
                     if (++cnt == cap) return false;
                 }
             }
@@ -995,12 +1007,25 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // phase 2: lambda over the list just written (L2-resident; plain loads,
     // the read-only path may not see this kernel's own stores)
     LamSum ls;
-    const uint32_t *rd = nl;
+    if (SMEM) {  // the list from shared memory, written out slot by slot as it is summed
+        const uint32_t *rd = s_list + threadIdx.x;
+        uint32_t *wr = nl;
 #pragma unroll 4
-    for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t q = *rd;
-        rd += stride;
-        ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t q = *rd;
+            rd += blockDim.x;
+            *wr = q;
+            wr += stride;
+            ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
+        }
+    } else {
+        const uint32_t *rd = nl;
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t q = *rd;
+            rd += stride;
+            ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
+        }
     }
     a.lam[i] = ls.lambda(d);
     TILE_LOOP_END
@@ -1594,9 +1619,20 @@ struct PassFns {
     if ((chunk) == 4) PassFns<4>::CALL; \
     else PassFns<8>::CALL;
 
-// Resident blocks per SM for the heaviest tile kernels at this block size.
+// Resident blocks per SM of each kernel at a tile size (cached per device,
+// tile and chunk: the step asks for its launch shape every time it runs).
 Occupancy occupancy(uint32_t tile, uint32_t chunk)
 {
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, uint32_t>, Occupancy> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, tile, chunk);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
     auto occ_b = [](const void *fn, uint32_t block) -> uint32_t {
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, (int)block, 0);
@@ -1609,13 +1645,17 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
                  mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
     o.cells = occ_b((const void *)k_rank_cells, kCellTile);
     o.split = occ_b((const void *)k_neighbors_split, 256);
-    o.nb = occ((const void *)k_neighbors_lambda);
+    o.nb = occ((const void *)k_neighbors_lambda<false>);
+    cudaFuncSetAttribute((const void *)k_neighbors_lambda<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kNbSmemMax);
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
     o.dp = occ(c4 ? PassFns<4>::dp() : PassFns<8>::dp());
     o.omega = occ((const void *)k_vort_omega<false>);
     o.apply = occ((const void *)k_vort_apply<false>);
     o.xsph = occ((const void *)k_xsph<false>);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = o;
     return o;
 }
 
@@ -1692,7 +1732,10 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
         k_neighbors_split<<<sh.grid_split, 256, 0, st>>>(a, sh.tile);
         PBF_LAUNCHED("k_neighbors_split");
     } else {
-        k_neighbors_lambda<<<sh.grid_nb, b, 0, st>>>(a);
+        if (sh.nb_smem)
+            k_neighbors_lambda<true><<<sh.grid_nb, b, sh.nb_smem, st>>>(a);
+        else
+            k_neighbors_lambda<false><<<sh.grid_nb, b, 0, st>>>(a);
         PBF_LAUNCHED("k_neighbors_lambda");
     }
     const bool xsph = (post & (kPostXsphWalk | kPostXsphList)) != 0;
