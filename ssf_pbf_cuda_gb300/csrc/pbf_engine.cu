@@ -638,20 +638,31 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.tile = tile;
     sh.chunk = chunk_;
     const Occupancy o = occupancy(tile, chunk_);
+    // Grids follow the tile counts rounded up to a power of two: every kernel
+    // loops over the device-resident counts (surplus blocks exit at once), so
+    // a captured graph survives scenes coming and going until a count
+    // crosses a power of two (a served stream changes its scene set many
+    // times a second).
+    auto pow2 = [](uint32_t v) {
+        uint32_t p = 1;
+        while (p < v) p <<= 1;
+        return p;
+    };
     const uint32_t nt = std::max<uint32_t>(1, ctrl_.n_tiles);
-    auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), nt); };
+    const uint32_t ntb = pow2(nt);
+    auto g = [&](uint32_t bps) { return std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, bps), ntb); };
     sh.grid = g(o.light);
-    sh.grid_nb = nt;  // a block per tile: the walk's cost varies per tile, and fresh blocks balance it
+    sh.grid_nb = ntb;  // a block per tile: the walk's cost varies per tile, and fresh blocks balance it
     sh.grid_lambda = g(o.lambda);
     sh.grid_dp = g(o.dp);
     sh.grid_omega = g(o.omega);
     sh.grid_apply = g(o.apply);
     sh.grid_xsph = g(o.xsph);
-    sh.grid_cells = std::max<uint32_t>(1, ctrl_.n_cell_tiles);  // a block per cell tile
+    sh.grid_cells = pow2(std::max<uint32_t>(1, ctrl_.n_cell_tiles));  // a block per cell tile
     sh.small = (uint64_t)nt * tile <= kSmallStep ? 1u : 0u;
-    sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), nt * (tile / (256 / kSplit)));
+    sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), ntb * (tile / (256 / kSplit)));
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
-    sh.scan_grid = std::min<uint32_t>(scan_tiles, (uint32_t)sms_ * 8);
+    sh.scan_grid = std::min<uint32_t>(pow2(scan_tiles), (uint32_t)sms_ * 8);
     if (ctrl_.n_cells <= kSingleScanMax) sh.scan_grid = 0;  // one-block scan
     {  // the block's lists in shared memory when they fit
         const uint64_t b = (uint64_t)tile * (max_pair_ - 1u) * 4u;
