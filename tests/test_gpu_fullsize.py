@@ -114,3 +114,17 @@ def test_one_block_scan_every_table_size(oracle, gpu, grid):
     assert 0 < ne.sum() < C
     assert np.array_equal(d["cell_start"] != 0xFFFFFFFF, ne)
     assert np.array_equal(d["cell_start"][ne], off[:C][ne]) and np.array_equal(d["cell_end"][ne], off[1:C + 1][ne])
+
+
+@pytest.mark.parametrize("max_pair", [30, 64, 100])
+def test_large_step_list_slots(oracle, gpu, max_pair):
+    """A large step (147,456 particles) collects each block's neighbour lists
+    in shared memory when they fit (tile x slots x 4 B: 29.7 KB, 64.5 KB past
+    the default 48 KB limit) and stores them directly when they do not
+    (101 KB): in every case hashes, permutation, cell ranges and neighbour
+    lists equal the oracle's."""
+    sc = scenes.dam_break(64, 48, 48, (8.0, 4.0, 4.0), scene_id=90 + max_pair)
+    params = api.config_params(max_pair_particle_num=max_pair, scorr_k=1e-4)
+    g = H.run_gpu(sc, params, "planes", iters=1)
+    r = H.run_oracle(oracle, sc, params, "planes", iters=1)
+    H.assert_integer_parity(g, r, H.resolved(params, sc))
