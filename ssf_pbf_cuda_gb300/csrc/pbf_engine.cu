@@ -164,7 +164,7 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
 uint64_t bytes_per_particle(uint32_t max_pair)
 {
     // x v xs xa xb xold w vt wx (float4) + key slot tmp perm id id_tmp wpos + lam + nnb + cls + nbr
-    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 4ull * (max_pair - 1);
+    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 16ull * ((max_pair - 1 + 3) / 4);  // list slots in whole quads
 }
 
 // ---------------------------------------------------------------- batch --
@@ -221,7 +221,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_offsets_, 4 * (C + 4)));
     CK(A((void **)&d_bsum_, 4 * ((C + kScanTile - 1) / kScanTile + 4)));
     CK(A((void **)&d_lam_, 4 * P));
-    CK(A((void **)&d_nbr_, 4ull * (max_pair - 1) * P));
+    CK(A((void **)&d_nbr_, 16ull * ((max_pair - 1 + 3) / 4) * P));  // quads of 4 slots per particle
     CK(A((void **)&d_nnb_, P));
     CK(A((void **)&d_cls_, P));
     CK(A((void **)&d_dense_, 4 * (2 * (P / 64 + 1) + 1)));  // a dense bucket holds more than 64 particles
@@ -976,14 +976,16 @@ pbf_status Batch::get_debug(uint32_t id, uint32_t *sorted_hash, uint32_t *perm, 
         const uint64_t padded = ((uint64_t)live + 31) / 32 * 32;
         std::fill(neighbor_list, neighbor_list + padded * mp, 0xFFFFFFFFu);
         std::vector<uint8_t> nn(live);
-        std::vector<uint32_t> row(live);
+        std::vector<uint32_t> quads(4ull * live);
         if (live) CK(cudaMemcpy(nn.data(), d_nnb_ + d.p_off, live, cudaMemcpyDeviceToHost));
-        for (uint32_t k = 0; k < d.cap && live; ++k) {
-            CK(cudaMemcpy(row.data(), d_nbr_ + (uint64_t)k * max_particles_ + d.p_off, 4ull * live,
+        for (uint32_t kq = 0; 4 * kq < d.cap && live; ++kq) {  // slots 4kq..4kq+3 of every particle
+            CK(cudaMemcpy(quads.data(), d_nbr_ + 4ull * ((uint64_t)kq * max_particles_ + d.p_off), 16ull * live,
                           cudaMemcpyDeviceToHost));
-            for (uint32_t p = 0; p < live; ++p)
-                if (k < nn[p])
-                    neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp] = row[p] - d.p_off;
+            for (uint32_t k = 4 * kq; k < 4 * kq + 4 && k < d.cap; ++k)
+                for (uint32_t p = 0; p < live; ++p)
+                    if (k < nn[p])
+                        neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp] =
+                            quads[4ull * p + (k & 3)] - d.p_off;
         }
     }
     return PBF_SUCCESS;

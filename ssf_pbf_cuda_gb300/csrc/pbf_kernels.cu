@@ -364,33 +364,51 @@ __device__ __forceinline__ void walk27_batched(const SceneDesc &d, const uint32_
     for (int k = 0; k < nb; ++k) use(buf[k]);
 }
 
-// Visit list slots [0, nn) of one particle in list order (slot-major
-// layout: slot k of particle i at nl[k * stride], nl = nbr + i).  Indices are
-// requested CH at a time, one chunk ahead of their use; the chunk (loads in
-// flight against registers) is picked by the autotuner.  Whole chunks call f
-// without per-slot predicates; only the index requests and the final partial
-// chunk test k < nn.
+// The neighbour list is stored in quads of slots: slot k of particle slot i
+// at nbr[(k / 4 * stride + i) * 4 + k % 4] (stride = particle slots), so a
+// thread's four consecutive slots are one aligned 16-byte load and the
+// quads of a warp's particles lie side by side (coalesced).  list_of is a
+// particle's base, list_slot the offset of its slot k.
+__device__ __forceinline__ uint32_t *list_of(uint32_t *nbr, uint32_t i) { return nbr + 4ull * i; }
+__device__ __forceinline__ uint64_t list_slot(uint32_t k, uint64_t stride)
+{
+    return (uint64_t)(k >> 2) * stride * 4u + (k & 3u);
+}
+
+__device__ __forceinline__ uint32_t quad_at(const uint4 &v, int j)
+{
+    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// Visit list slots [0, nn) of one particle in list order.  Indices are
+// requested CH at a time (CH / 4 quads), one chunk ahead of their use; the
+// chunk (loads in flight against registers) is picked by the autotuner.
+// Whole chunks call f without per-slot predicates; only the quad requests
+// and the final partial chunk test against nn.
 template <int CH, class F>
 __device__ __forceinline__ void list_walk(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn, F &&f)
 {
-    uint32_t qn[CH];
-    const uint32_t *p = nl;
+    static_assert(CH % 4 == 0, "a chunk holds whole quads");
+    constexpr int NQ = CH / 4;
+    const uint4 *p = reinterpret_cast<const uint4 *>(nl);  // quad kq of the particle at p[kq * stride]
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    uint4 qn[NQ];
 #pragma unroll
-    for (int c = 0; c < CH; ++c) qn[c] = ((uint32_t)c < nn) ? __ldg(p + c * stride) : 0u;
+    for (int c = 0; c < NQ; ++c) qn[c] = ((uint32_t)(4 * c) < nn) ? __ldg(p + c * stride) : z;
     uint32_t k0 = 0;
     for (; k0 + CH <= nn; k0 += CH) {
-        uint32_t q[CH];
+        uint4 q[NQ];
 #pragma unroll
-        for (int c = 0; c < CH; ++c) q[c] = qn[c];
-        p += CH * stride;
+        for (int c = 0; c < NQ; ++c) q[c] = qn[c];
+        p += NQ * stride;
 #pragma unroll
-        for (int c = 0; c < CH; ++c) qn[c] = (k0 + CH + c < nn) ? __ldg(p + c * stride) : 0u;
+        for (int c = 0; c < NQ; ++c) qn[c] = (k0 + CH + 4 * c < nn) ? __ldg(p + c * stride) : z;
 #pragma unroll
-        for (int c = 0; c < CH; ++c) f(q[c]);
+        for (int c = 0; c < CH; ++c) f(quad_at(q[c >> 2], c & 3));
     }
 #pragma unroll
     for (int c = 0; c < CH - 1; ++c)
-        if (k0 + c < nn) f(qn[c]);
+        if (k0 + c < nn) f(quad_at(qn[c >> 2], c & 3));
 }
 
 // Per-tile prologue shared by the particle kernels.
@@ -973,7 +991,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     const float h2 = d.h2, inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
     const uint32_t cap = d.cap;
     const uint64_t stride = a.nbr_stride;
-    uint32_t *nl = a.nbr + i;
+    uint32_t *nl = list_of(a.nbr, i);
     const float4 *__restrict__ xa = a.xa;
     const float4 *__restrict__ wx = a.wx;
     // phase 1: the walk only tests and records (lanes of a warp accept
@@ -983,8 +1001,6 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // tested in order, so the first `cap` accepted ones are the reference's.
     constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
-    uint32_t *slot = SMEM ? s_list + threadIdx.x : nl;
-    const uint32_t slot_step = SMEM ? blockDim.x : (uint32_t)stride;
     walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
                        [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
@@ -995,8 +1011,10 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
-                    *slot = __float_as_uint(c[k].w);
-                    slot += slot_step;
+                    if (SMEM)
+                        s_list[cnt * blockDim.x + threadIdx.x] = __float_as_uint(c[k].w);
+                    else
+                        nl[list_slot(cnt, stride)] = __float_as_uint(c[k].w);
                     if (++cnt == cap) return false;
                 }
             }
@@ -1008,22 +1026,26 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // the read-only path may not see this kernel's own stores)
     LamSum ls;
     if (SMEM) {  // the list from shared memory, written out slot by slot as it is summed
+        // the list out in whole quads: one 16-byte store per four slots
+        // (slots past the count in the last quad are padding, never read)
         const uint32_t *rd = s_list + threadIdx.x;
-        uint32_t *wr = nl;
+        uint4 *wq = reinterpret_cast<uint4 *>(nl);
+        for (uint32_t k0 = 0; k0 < cnt; k0 += 4) {
+            uint32_t q4[4];
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) q4[j] = (k0 + j < cnt) ? rd[(k0 + j) * blockDim.x] : 0u;
+            wq[(uint64_t)(k0 >> 2) * stride] = make_uint4(q4[0], q4[1], q4[2], q4[3]);
+        }
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
             const uint32_t q = *rd;
             rd += blockDim.x;
-            *wr = q;
-            wr += stride;
             ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
         }
     } else {
-        const uint32_t *rd = nl;
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t q = *rd;
-            rd += stride;
+            const uint32_t q = nl[list_slot(k, stride)];
             ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
         }
     }
@@ -1063,7 +1085,7 @@ template <bool RO>
 __device__ __forceinline__ uint32_t split_index(const uint32_t *nl, uint64_t stride, uint32_t nn, uint32_t k)
 {
     if (k >= nn) return 0u;
-    const uint32_t *p = nl + (uint64_t)k * stride;
+    const uint32_t *p = nl + list_slot(k, stride);
     return RO ? __ldg(p) : *p;
 }
 
@@ -1116,7 +1138,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         const float h2 = d.h2;
         const uint32_t cap = d.cap;
         const uint64_t stride = a.nbr_stride;
-        uint32_t *nl = a.nbr + i;
+        uint32_t *nl = list_of(a.nbr, i);
         const float4 *__restrict__ xa = a.xa;
         const float4 *__restrict__ wx = a.wx;
         // rows shared over the lanes (split_rows); one lane takes all nine
@@ -1132,7 +1154,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
                 for (uint32_t q = st; q < en; ++q) {
                     const float4 c = __ldg(src + q);
                     if (dist2_exact(xp, c) < h2) {
-                        nl[(uint64_t)cnt * stride] = __float_as_uint(c.w);
+                        nl[list_slot(cnt, stride)] = __float_as_uint(c.w);
                         if (++cnt == cap) return false;
                     }
                 }
@@ -1167,7 +1189,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         const uint32_t total = __shfl_sync(gmask, incl, kSplit - 1, kSplit);
         if (!one) {
             const uint32_t pre = incl - cnt;
-            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) nl[(uint64_t)(pre + t) * stride] = buf[t];
+            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) nl[list_slot(pre + t, stride)] = buf[t];
         }
         const uint32_t nn = total < cap ? total : cap;
         __syncwarp(gmask);  // the list entries of the group are visible to all its lanes
@@ -1196,7 +1218,7 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
     const float4 xp = xc[i];
     LamSum ls;
-    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i],
+    list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i],
                       [&](uint32_t q) { ls.add(pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta)); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
     // delta-p pass gathers next (neighbours here use only .xyz); small,
@@ -1263,7 +1285,7 @@ __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, 
     const ScorrConst sc = scorr_const(d, li);
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    list_walk<kChunk>(a.nbr + i, a.nbr_stride, a.nnb[i], [&](uint32_t q) {
+    list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], [&](uint32_t q) {
         const float4 xq = __ldg(xc + q);
         const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
         const float lj = LAMW ? xq.w : __ldg(lam + q);  // LAMW: lambda in .w of the positions
@@ -1386,7 +1408,7 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             },
             use);
     } else {
-        list_walk<8>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
     }
     const float mr = d.m * d.inv_rho0;
     const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
@@ -1438,7 +1460,7 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             },
             use);
     } else {
-        list_walk<4>(a.nbr + i, a.nbr_stride, a.nnb[i], use);  // 4: fewer registers, more warps (measured)
+        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);  // 4: fewer registers, more warps (measured)
     }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
@@ -1520,7 +1542,7 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
             },
             use);
     } else {
-        list_walk<8>(a.nbr + i, a.nbr_stride, a.nnb[i], use);
+        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
     }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
