@@ -971,11 +971,10 @@ __global__ void __launch_bounds__(512) k_gather(StepArgs a)
 // (calcScalingFactorCUDA cached, pbf_constraint.cu:168-209): at iteration 0
 // the working positions are the sorted predicted positions, so the pair
 // terms can be summed while the list is built.
-// SMEM: the accepted indices are collected in shared memory (slot-major per
-// block, conflict-free) and written to the list by the lambda loop that
-// reads them back, so every list store of a warp is coalesced (the lanes'
-// slot k at consecutive particles) instead of one scattered 4-byte store per
-// accepted candidate.
+// SMEM: the accepted indices are collected in shared memory ([slot][thread]
+// per block, conflict-free), then written to the list in whole quads (a
+// warp's 16-byte stores contiguous) instead of one scattered 4-byte store per
+// accepted candidate, and the lambda loop reads them back from shared memory.
 template <bool SMEM>
 __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 {
