@@ -411,6 +411,31 @@ __device__ __forceinline__ void list_walk(const uint32_t *__restrict__ nl, uint6
         if (k0 + c < nn) f(quad_at(qn[c >> 2], c & 3));
 }
 
+// list_walk in chunks of one quad with the quads requested two chunks
+// ahead: eight indices in flight, one quad of them per use.
+template <class F>
+__device__ __forceinline__ void list_walk_ahead2(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn,
+                                                 F &&f)
+{
+    const uint4 *p = reinterpret_cast<const uint4 *>(nl);
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    uint4 q0 = (0u < nn) ? __ldg(p) : z;
+    uint4 q1 = (4u < nn) ? __ldg(p + stride) : z;
+    uint32_t k0 = 0;
+    for (; k0 + 4 <= nn; k0 += 4) {
+        const uint4 q = q0;
+        q0 = q1;
+        q1 = (k0 + 8 < nn) ? __ldg(p + (uint64_t)((k0 >> 2) + 2) * stride) : z;
+        f(q.x);
+        f(q.y);
+        f(q.z);
+        f(q.w);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        if (k0 + c < nn) f(quad_at(q0, c));
+}
+
 // Per-tile prologue shared by the particle kernels.
 #define TILE_LOOP_BEGIN                                                   \
     const uint32_t n_tiles_ = a.ctrl->n_tiles;                            \
@@ -1541,7 +1566,7 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
             },
             use);
     } else {
-        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
+        list_walk_ahead2(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
     }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
