@@ -191,14 +191,19 @@ pbf_status pbf_get_neighbor_debug(pbf_handle *h, uint32_t *sorted_hash, uint32_t
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need the sort (code running under CUDA-graph stream
  * capture, plug-ins whose host owns all device allocations, real-time paths):
- * cell hash of x (n x 3 floats, device), stable counting sort by cell, and
- * cell ranges, exactly as pbf_one_step computes them for its predicted
- * positions.  perm_dev[n] receives sorted -> input index; cell_start_dev /
- * cell_end_dev [Gx*Gy*Gz] the ranges (0xFFFFFFFF for empty cells).  Needs no
- * handle and allocates nothing: its scratch is a fixed device array (7.3 MB)
- * that every GPU loading the library holds until exit.  Larger inputs return
- * PBF_ERROR_CAPACITY.  The first call on a device looks the array up and
- * should come before any stream capture; calls that overlap on the GPU share
+ * cell hash of x (n x 3 floats, device), stable counting sort by cell (a
+ * cell's particles in ascending input index, at any bucket size), and cell
+ * ranges, as pbf_one_step computes them for its predicted positions of a
+ * scene whose simulation area holds every particle: there is no area check
+ * here, so a particle outside the area is not deleted but hashed into the
+ * wrapped table like any other.  perm_dev[n] receives sorted -> input index;
+ * cell_start_dev / cell_end_dev [Gx*Gy*Gz] the ranges (0xFFFFFFFF for empty
+ * cells).  Needs no handle and allocates nothing: its scratch is a fixed
+ * device array (7.3 MB) that every GPU loading the library holds until exit.
+ * Larger inputs return PBF_ERROR_CAPACITY.  The first call on a device looks
+ * the array up and should come before any stream capture; the address is
+ * kept for the life of the process, so after a cudaDeviceReset the process
+ * must not call this entry point again.  Calls that overlap on the GPU share
  * the array and race, so the caller serialises them. */
 #define PBF_NOALLOC_MAX_PARTICLES 262144u
 #define PBF_NOALLOC_MAX_CELLS 524288u

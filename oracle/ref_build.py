@@ -11,7 +11,21 @@ changes, which this recipe applies to a scratch copy under oracle/_ref/src
      a temporary, accepted only by MSVC) becomes `auto grid_size = ...`
      in pbf_xsph.cu and pbf_vorticity_confinement.cu;
   4. GLM_FORCE_CUDA is not defined (GLM 0.9.7 rejects CUDA 13 with it).
-The copy is made where the reference is mounted (prepare); the build runs
+Two more, active only in the "cub" variant (-DUSE_CUB, the reference's
+stable cub::DeviceRadixSort::SortPairs path, pbf_neighbor_search.cpp:123-131),
+which does not compile as shipped:
+  5. the detectNeighbors overload that path calls (with the sorted hash and
+     index arrays, pbf_neighbor_search.cpp:129-131) is missing from
+     pbf_neighbor_search_util.h:67-73; a forwarding overload is appended
+     (the kernel it would launch ignores those arrays: it is passed nullptr
+     for them, pbf_neighbor_search_util.cu:868-869);
+  6. the radix sort's temporary storage is sized as the commented-out lines
+     pbf_neighbor_search.cpp:39-41 did, instead of the counting sort's scan
+     storage (:44-46).
+That path skips deletion (pbf_neighbor_search.cpp:146-159), so it is run only
+on scenes that keep every particle inside the simulation area.
+The copy is made where the reference is mounted (prepare; the location comes
+from $PBF_REFERENCE_ROOT or --root, default /root/reference); the build runs
 wherever nvcc is (a machine of another architecture builds its own binary from the copy).
 Outputs go only to oracle/_ref/.  The reference's own build files are not used.
 """
@@ -25,7 +39,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("PBF_REFERENCE_ROOT", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 PBF_REL = os.path.join("cuda_pbf_with_ssf", "src", "pbf")
@@ -42,7 +56,32 @@ VARIANTS = {
     "ieee": [],
     # the shipped flags (cuda_pbf_with_ssf.vcxproj:125-127)
     "fast": ["-use_fast_math", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+    # IEEE, with the stable radix-sort path (changes 5 and 6 above)
+    "cub": ["-DUSE_CUB"],
 }
+
+# change 5: appended inside namespace pbf::cuda of pbf_neighbor_search_util.h
+CUB_OVERLOAD = """
+#ifdef USE_CUB
+// test-side shim: the overload pbf_neighbor_search.cpp calls under USE_CUB
+inline void detectNeighbors(uint32_t *neighbor_list, const dom_dim *position, const uint32_t *, const uint32_t *,
+                            const uint32_t *cell_start, const uint32_t *cell_end, scalar_t cell_width,
+                            dom_udim grid_size, scalar_t h, uint32_t num_particle, uint32_t max_pair_particle_num)
+{
+    detectNeighbors(neighbor_list, position, cell_start, cell_end, cell_width, grid_size, h, num_particle,
+                    max_pair_particle_num);
+}
+#endif
+"""
+# change 6: the scan-storage sizing line of the neighbor_search constructor
+SCAN_SIZING = "cuda::getPrefixSumStorageSize(temp_cub_storage_size, cell_num);"
+CUB_SIZING = """
+#ifdef USE_CUB
+	cuda::getRadixSortStorageSize(temp_cub_storage_size, max_particle_num);
+#else
+	cuda::getPrefixSumStorageSize(temp_cub_storage_size, cell_num);
+#endif
+"""
 
 
 def present() -> bool:
@@ -71,6 +110,13 @@ def prepare() -> bool:
             s2 = inc.sub(lambda m: m.group(1) + m.group(2).replace("\\", "/") + m.group(3), s)
             s2 = s2.replace("auto& grid_size = ns->getGridSize();", "auto grid_size = ns->getGridSize();")
             s2 = s2.replace("auto& grid_size = ns.getGridSize();", "auto grid_size = ns.getGridSize();")
+            if fn == "pbf_neighbor_search_util.h":
+                tail = "}\t// end of cuda ns"
+                assert s2.count(tail) == 1, "pbf_neighbor_search_util.h: namespace end not found"
+                s2 = s2.replace(tail, CUB_OVERLOAD + tail)
+            if fn == "pbf_neighbor_search.cpp":
+                assert s2.count(SCAN_SIZING) == 1, "pbf_neighbor_search.cpp: scan sizing not found"
+                s2 = s2.replace(SCAN_SIZING, CUB_SIZING)
             if s2 != s:
                 open(p, "w", encoding="latin-1").write(s2)
     return True
@@ -101,6 +147,11 @@ def build(variant: str = "ieee", jobs: int = 16) -> str:
     flags = ["-O2", "-std=c++17", "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a",
              "-I", SRC, "-I", os.path.join(SRC, "include"), "-w", *VARIANTS[variant]]
     srcs = sources() + [os.path.join(HERE, "ref_driver.cu")]
+    exe = binary(variant)
+    if os.path.exists(exe) and os.path.getmtime(exe) > max(os.path.getmtime(s) for s in srcs + [__file__]):
+        # built from these sources already (the binary runs only where it was built:
+        # a machine of another architecture has none)
+        return exe
     objs = []
 
     def cc(s):
@@ -129,6 +180,8 @@ def build_if_present() -> None:
 
 
 if __name__ == "__main__":
+    if "--root" in sys.argv:
+        REF_ROOT = sys.argv[sys.argv.index("--root") + 1]
     if "--prepare" in sys.argv or present():
         prepare()
     for v in ([a for a in sys.argv[1:] if a in VARIANTS] or ["ieee"]):

@@ -6,8 +6,22 @@
 // to the reference's results.  Private members of neighbor_search are read
 // for the sorted hash/index arrays (src/pbf/interaction/pbf_neighbor_search.h:69-89).
 //
+// post selects the velocity update after the solver iterations:
+//   0  one_step as shipped: the vorticity overload of update, whose XSPH and
+//      vorticity calls are commented out (pbf_solve.cpp:125-145);
+//   1  the XSPH overload of update (pbf_solve.cpp:108-123): updateVelocity,
+//      applyXSPH (src/pbf/solver/cuda/pbf_xsph.cu:120-152), updatePosition;
+//   2  the vorticity overload with its commented calls active, in their
+//      order (pbf_solve.cpp:134-141): updateVelocity, calcVorticity,
+//      addVorticityConfinement (pbf_vorticity_confinement.cu:229-296),
+//      applyXSPH, updatePosition;
+//   3  the same without applyXSPH (velocity copied as pbf_solve.cpp:142).
+// For post != 0 the driver runs one_step's body itself (predict,
+// detectNeighbors, solveConstraint as pbf_solve.cpp:154-176 / 186-211).
+//
 // Input (little endian): "PBFI", u32 version, u32 n, u32 capacity, i32 iters,
-//   i32 use_boundary, f32 params[8] (pbf_parameter order), f32 body_force[3],
+//   i32 use_boundary, [version >= 2: i32 post], f32 params[8] (pbf_parameter
+//   order), f32 body_force[3],
 //   f32 domain_end[3], f32 area_min[3], f32 area_max[3], u32 n_inner, n_outer,
 //   n_planes, f32 inner[4 n_inner], outer[4 n_outer], pts[3 n_planes],
 //   nrm[3 n_planes], f32 x[3n], v[3n].
@@ -25,7 +39,18 @@
 #define private public
 #include "pbf/pbf.h"
 #include "pbf/interaction/pbf_neighbor_search.h"
+#include "pbf/solver/cuda/pbf_update.h"
 #undef private
+
+namespace pbf {
+// the boundary overload of the cached solveConstraint: defined in
+// src/pbf/solver/pbf_solve.cpp:79-106, not declared in its header
+void solveConstraint(dom_dim *interim_position, dom_dim *position_update, scalar_t *scaling_factor,
+                     scalar_t *kernels, dom_dim *grad_kernels, const dom_dim *old_position,
+                     const pbf_boundary &boundary, std::shared_ptr<neighbor_search> &ns,
+                     scalar_t inv_stable_density, scalar_t particle_mass, scalar_t smoothing_length,
+                     scalar_t relaxation, int num_iteration, int num_particle);
+}  // namespace pbf
 
 template <class T>
 static void rd(FILE *f, T *p, size_t n)
@@ -62,12 +87,17 @@ int main(int argc, char **argv)
     rd(f, magic, 4);
     if (memcmp(magic, "PBFI", 4)) return 1;
     uint32_t ver, n, cap;
-    int32_t iters, use_b;
+    int32_t iters, use_b, post = 0;
     rd(f, &ver, 1);
     rd(f, &n, 1);
     rd(f, &cap, 1);
     rd(f, &iters, 1);
     rd(f, &use_b, 1);
+    if (ver >= 2) rd(f, &post, 1);
+    if (post < 0 || post > 3) {
+        fprintf(stderr, "post mode %d\n", post);
+        return 1;
+    }
     float prm[8], g[3], dend[3], amin[3], amax[3];
     rd(f, prm, 8);
     rd(f, g, 3);
@@ -114,8 +144,47 @@ int main(int argc, char **argv)
     }
     pbf_boundary bnd;
     if (use_b) bnd.allocate(in, out, pp, pn);
+    // one_step's body with the post-solve update chosen by `post`
+    auto step_post = [&]() {
+        cudaDeviceSetCacheConfig(cudaFuncCachePreferL1);
+        auto &phase = part.phase;
+        auto &param = part.parameter;
+        auto ns = part.ns;
+        uint32_t &num = part.phase.num;
+        const auto inv_rho0 = 1.f / param.stable_density;
+        const auto m = param.particle_mass;
+        const auto h = param.smoothing_length;
+        const auto inv_t = 1.f / param.time_step;
+        pbf::predict(buf.interim.x, buf.interim.v, phase.x, phase.v, part.external.body_force, param.time_step,
+                     num);
+        ns->detectNeighbors(buf.sorted_predicted_pos, buf.interim.x, buf.sorted_old_pos, phase.x, h, area, num);
+        if (use_b)
+            pbf::solveConstraint(buf.sorted_predicted_pos, buf.delta_position, buf.scaling_factor, buf.kernels,
+                                 buf.grad_kernels, buf.sorted_old_pos, bnd, ns, inv_rho0, m, h, param.relaxation,
+                                 iters, num);
+        else
+            pbf::solveConstraint(buf.sorted_predicted_pos, buf.delta_position, buf.scaling_factor, buf.kernels,
+                                 buf.grad_kernels, buf.sorted_old_pos, ns, inv_rho0, m, h, param.relaxation, iters,
+                                 num);
+        if (post == 1) {
+            pbf::update(phase.x, phase.v, buf.interim.v, buf.sorted_predicted_pos, buf.sorted_old_pos, ns, inv_t,
+                        inv_rho0, m, h, param.xsph_parameter, num);
+            return;
+        }
+        pbf::cuda::updateVelocity(buf.interim.v, buf.sorted_predicted_pos, buf.sorted_old_pos, inv_t, num);
+        pbf::cuda::calcVorticity(buf.vorticity, buf.sorted_predicted_pos, buf.interim.v, *ns, h, m, inv_rho0, num);
+        pbf::cuda::addVorticityConfinement(buf.interim.v, buf.vorticity, buf.sorted_predicted_pos, *ns, h, m,
+                                           inv_rho0, param.vc_parameter, 1.f / inv_t, num);
+        if (post == 2)
+            pbf::cuda::applyXSPH(phase.v, buf.sorted_predicted_pos, buf.interim.v, ns, h, param.xsph_parameter,
+                                 inv_rho0, m, num);
+        else
+            pbf::cuda::updateVelocity(phase.v, buf.interim.v, num);
+        pbf::cuda::updatePosition(phase.x, buf.sorted_predicted_pos, num);
+    };
     auto step = [&]() {
-        if (use_b) pbf::one_step(part, buf, bnd, area, iters);
+        if (post) step_post();
+        else if (use_b) pbf::one_step(part, buf, bnd, area, iters);
         else pbf::one_step(part, buf, area, iters);
     };
     if (reps > 0) {

@@ -24,7 +24,7 @@ SOURCES = ["pbf_kernels.cu", "pbf_engine.cu", "pbf_capi.cu", "pbf_server.cu", "p
 # per-file flags: the screen-space passes round every product and sum on its
 # own (no contraction into FMA), as their CPU restatement does
 FILE_FLAGS = {"pbf_ssf.cu": ["-fmad=false"]}
-HEADERS = ["pbf_internal.h", "pbf_engine.h"]
+HEADERS = ["pbf_internal.h", "pbf_engine.h", "pbf_sort.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

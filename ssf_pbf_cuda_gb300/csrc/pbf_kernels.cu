@@ -20,6 +20,7 @@
 #include <tuple>
 
 #include "pbf_internal.h"
+#include "pbf_sort.cuh"
 #include "pbf103.h"
 
 namespace pbf103 {
@@ -705,11 +706,12 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
 // bucket entries and the bucket's part of the permutation are read and
 // written contiguously whatever the particles' input order.  Buckets of up
 // to kMidMin members are ranked here; larger ones are queued for
-// k_dense_sort (a warp per bucket up to kDenseMin members, a block beyond).
-// Buckets larger than kStableLimit keep the atomic order (they only arise
-// from degenerate inputs or mass deletion).
+// k_dense_sort (a warp per bucket up to kDenseMin members, a block beyond:
+// a shared-memory sort up to kStableLimit members, a radix sort in global
+// memory above, which degenerate inputs and mass deletion can reach).
 constexpr uint32_t kStableLimit = 4096;
 constexpr uint32_t kDenseMin = 64;
+static_assert(kStableLimit * sizeof(uint32_t) == sizeof(RadixSmem), "the radix sort reuses the bitonic buffer");
 __global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
 {
     const uint32_t n0 = a.ctrl->n_tiles, nct = a.ctrl->n_cell_tiles;
@@ -726,7 +728,7 @@ __global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
         const uint32_t st = __ldg(a.offsets + gk), en = __ldg(a.offsets + gk + 1);
         if (st == en) continue;
         const uint32_t b = en - st;
-        if (b > kMidMin && b <= kStableLimit) {
+        if (b > kMidMin) {
             uint32_t *q = b > kDenseMin ? a.dense : a.mid;
             const uint32_t k = atomicAdd(q, 1u);
             q[1 + 2 * k] = gk;
@@ -735,14 +737,6 @@ __global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
         }
         const uint32_t g0 = p_off + (st - __ldg(a.offsets + c_off));
         const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
-        if (b > kStableLimit) {  // atomic order: entry t of the bucket came with slot t
-            for (uint32_t t = 0; t < b; ++t) {
-                a.perm[g0 + t] = __ldg(a.tmp + st + t) & imask;
-                a.wpos[g0 + t] = kNoWalkCopy;
-            }
-            a.chist[gk] = kClassWhole;
-            continue;
-        }
         // the alias class rides in the entries' top bits (scenes below 2^29
         // particles); the walk copy groups a bucket by class when the grid
         // is at least 4 cells on every axis
@@ -773,8 +767,9 @@ __global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
 // The same ranks from the particle side, for small steps (latency bound:
 // the per-cell kernel's b^2 loop in one thread lengthens the critical
 // path): each particle counts the smaller input indices of its bucket.
-// Buckets above kDenseMin members are queued for k_dense_sort by their
-// first member (atomic slot 0); nothing is queued for the warp tier.
+// Buckets above kDenseMin members (of any size) are queued for
+// k_dense_sort by their first member (atomic slot 0); nothing is queued for
+// the warp tier.
 __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
 {
     TILE_LOOP_BEGIN
@@ -790,11 +785,11 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
     const bool packed = d.capacity <= kClsLimit;
     const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
     const uint32_t my_cls = a.cls[i];
-    uint32_t rank, below = 0, frank = 0;
+    uint32_t rank = 0, below = 0, frank = 0;
     const bool grouped = packed && en - st <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
     uint64_t hist = (uint64_t)(en - st) << (8u * my_cls);  // every member of my class
     bool mixed = false;
-    if (en - st > kDenseMin && en - st <= kStableLimit) {
+    if (en - st > kDenseMin) {
         // a dense bucket: one block of k_dense_sort orders it; its first
         // member by atomic slot queues it
         if (a.slot[i] == 0) {
@@ -804,27 +799,22 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
         }
         continue;
     }
-    if (en - st <= kStableLimit) {
-        rank = 0;
-        uint32_t diff = 0;
+    uint32_t diff = 0;
+    for (uint32_t t = st; t < en; ++t) {
+        const uint32_t e = __ldg(a.tmp + t);
+        rank += ((e & imask) < local) ? 1u : 0u;
+        diff |= (e >> kClsShift) ^ my_cls;
+    }
+    if (grouped && diff) {  // several classes: the class histogram and my place in the walk copy
+        mixed = true;
+        hist = 0;
         for (uint32_t t = st; t < en; ++t) {
             const uint32_t e = __ldg(a.tmp + t);
-            rank += ((e & imask) < local) ? 1u : 0u;
-            diff |= (e >> kClsShift) ^ my_cls;
+            const uint32_t mc = e >> kClsShift;
+            below += (mc < my_cls) ? 1u : 0u;
+            frank += (mc == my_cls && (e & imask) < local) ? 1u : 0u;
+            hist += 1ull << (8u * mc);
         }
-        if (grouped && diff) {  // several classes: the class histogram and my place in the walk copy
-            mixed = true;
-            hist = 0;
-            for (uint32_t t = st; t < en; ++t) {
-                const uint32_t e = __ldg(a.tmp + t);
-                const uint32_t mc = e >> kClsShift;
-                below += (mc < my_cls) ? 1u : 0u;
-                frank += (mc == my_cls && (e & imask) < local) ? 1u : 0u;
-                hist += 1ull << (8u * mc);
-            }
-        }
-    } else {
-        rank = a.slot[i];
     }
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t g = d.p_off + (st - base) + rank;
@@ -846,7 +836,9 @@ __global__ void __launch_bounds__(512) k_rank_reorder(StepArgs a)
 // class in the top bits) are sorted in shared memory by input index (the
 // stable sorted order) and, when the bucket mixes classes, by (class, index)
 // (the walk copy's order).  Both give the permutation, class counts and
-// walk-copy places of k_rank_cells' per-bucket count.
+// walk-copy places of k_rank_cells' per-bucket count.  Buckets above
+// kStableLimit get a block each too: a radix sort by input index in global
+// memory (block_radix_stable), walked whole.
 __device__ __forceinline__ uint32_t dense_key(uint32_t e, uint32_t imask)
 {
     return e == 0xFFFFFFFFu ? 0xFFFFFFFFu : (e & imask);  // padding sorts last
@@ -872,10 +864,11 @@ __device__ void bitonic_sort(uint32_t *v, uint32_t n, uint32_t imask)
     }
 }
 
-__global__ void __launch_bounds__(256) k_dense_sort(StepArgs a)
+__global__ void __launch_bounds__(kRadixThreads) k_dense_sort(StepArgs a)
 {
-    __shared__ uint32_t S[kStableLimit], W[kStableLimit];
-    __shared__ uint32_t chist_cnt[8];
+    __shared__ __align__(16) uint32_t S[kStableLimit];
+    __shared__ uint32_t W[kStableLimit];
+    __shared__ uint32_t chist_cnt[8], rbase[16], rtot[16];
     {
         const uint32_t nm = *(volatile const uint32_t *)a.mid;
         const uint32_t lane = threadIdx.x & 31u, wpb = blockDim.x >> 5;
@@ -927,6 +920,14 @@ __global__ void __launch_bounds__(256) k_dense_sort(StepArgs a)
         const uint32_t g0 = d.p_off + (st - base);
         const bool packed = d.capacity <= kClsLimit;
         const uint32_t imask = packed ? kClsLimit - 1u : 0xFFFFFFFFu;
+        if (b > kStableLimit) {  // the bucket's scatter entries are scratch once sorted into perm
+            block_radix_stable(a.tmp + st, a.perm + g0, b, imask, radix_bits(d.capacity),
+                               *reinterpret_cast<RadixSmem *>(S), rbase, rtot);
+            for (uint32_t t = threadIdx.x; t < b; t += blockDim.x) a.wpos[g0 + t] = kNoWalkCopy;
+            if (threadIdx.x == 0) a.chist[gk] = kClassWhole;
+            __syncthreads();
+            continue;
+        }
         const bool grouped = packed && b <= 255u && d.gx >= 4 && d.gy >= 4 && d.gz >= 4;
         uint32_t P = 1;
         while (P < b) P <<= 1;
@@ -1770,7 +1771,7 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
         k_rank_cells<<<sh.grid_cells, kCellTile, 0, st>>>(a);
         PBF_LAUNCHED("k_rank_cells");
     }
-    k_dense_sort<<<sh.grid, 256, 0, st>>>(a);
+    k_dense_sort<<<sh.grid, kRadixThreads, 0, st>>>(a);
     PBF_LAUNCHED("k_dense_sort");
     k_gather<<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_gather");

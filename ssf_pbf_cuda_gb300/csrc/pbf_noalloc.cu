@@ -24,6 +24,7 @@
 
 #include "pbf103.h"
 #include "pbf_internal.h"
+#include "pbf_sort.cuh"
 
 namespace pbf103 {
 void set_last_error(const char *what, cudaError_t e);
@@ -35,13 +36,18 @@ constexpr uint32_t kMaxN = PBF_NOALLOC_MAX_PARTICLES;
 constexpr uint32_t kMaxC = PBF_NOALLOC_MAX_CELLS;
 constexpr uint32_t kTile = 4096;                            // cells per scan tile
 constexpr uint32_t kMaxTiles = (kMaxC + 1 + kTile - 1) / kTile;
-// words: keys, slots, tmp (n each); counts, offsets (C + 2 each); tile sums
-constexpr size_t kWords = 3ull * kMaxN + 2ull * (kMaxC + 2) + kMaxTiles + 4;
+// buckets of more than kRankMax entries are sorted by a block each
+// (block_radix_stable); at most kMaxBig of them fit in kMaxN particles
+constexpr uint32_t kRankMax = 4096;
+constexpr uint32_t kMaxBig = kMaxN / (kRankMax + 1) + 1;
+// words: keys, slots, tmp (n each); counts, offsets (C + 2 each); tile sums;
+// the queue of large buckets (count, then cells)
+constexpr size_t kWords = 3ull * kMaxN + 2ull * (kMaxC + 2) + kMaxTiles + 4 + 1 + kMaxBig;
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kWords];
 
 struct Scratch {
-    uint32_t *keys, *slots, *tmp, *counts, *offsets, *tsum;
+    uint32_t *keys, *slots, *tmp, *counts, *offsets, *tsum, *big;
 };
 
 Scratch carve(uint32_t *base)
@@ -53,6 +59,7 @@ Scratch carve(uint32_t *base)
     s.counts = s.tmp + kMaxN;
     s.offsets = s.counts + (kMaxC + 2);
     s.tsum = s.offsets + (kMaxC + 2);
+    s.big = s.tsum + kMaxTiles + 4;
     return s;
 }
 
@@ -92,9 +99,11 @@ __global__ void na_tile_sums(uint32_t C, Scratch s)
     if (threadIdx.x == 0) s.tsum[t] = part[0];
 }
 
-// one thread: exclusive scan of the (at most kMaxTiles) tile sums
+// one thread: exclusive scan of the (at most kMaxTiles) tile sums; empties
+// the large-bucket queue that na_rank fills next
 __global__ void na_tile_scan(uint32_t ntiles, uint32_t C, Scratch s)
 {
+    s.big[0] = 0;
     uint32_t run = 0;
     for (uint32_t t = 0; t < ntiles; ++t) {
         const uint32_t v = s.tsum[t];
@@ -140,19 +149,36 @@ __global__ void na_scatter(uint32_t n, Scratch s)
     if (i < n) s.tmp[s.offsets[s.keys[i]] + s.slots[i]] = i;
 }
 
-// stable position = bucket start + number of smaller indices in the bucket
+// stable position = bucket start + number of smaller indices in the bucket;
+// a bucket above kRankMax entries is queued (by its member of atomic slot 0)
+// for na_big instead
 __global__ void na_rank(uint32_t n, Scratch s, uint32_t *__restrict__ perm)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = s.keys[i];
     const uint32_t st = s.offsets[k], en = s.offsets[k + 1];
-    uint32_t r = s.slots[i];  // buckets above 4096 entries keep the atomic order
-    if (en - st <= 4096) {
-        r = 0;
-        for (uint32_t t = st; t < en; ++t) r += (s.tmp[t] < i) ? 1u : 0u;
+    if (en - st > kRankMax) {
+        if (s.slots[i] == 0) s.big[1 + atomicAdd(s.big, 1u)] = k;
+        return;
     }
+    uint32_t r = 0;
+    for (uint32_t t = st; t < en; ++t) r += (s.tmp[t] < i) ? 1u : 0u;
     perm[st + r] = i;
+}
+
+// the queued large buckets, a block each: stable order by input index
+__global__ void __launch_bounds__(pbf103::kRadixThreads) na_big(uint32_t n, Scratch s, uint32_t *__restrict__ perm)
+{
+    __shared__ pbf103::RadixSmem sm;
+    __shared__ uint32_t base[16], tot[16];
+    const uint32_t nb = s.big[0];
+    for (uint32_t q = blockIdx.x; q < nb; q += gridDim.x) {
+        const uint32_t k = s.big[1 + q];
+        const uint32_t st = s.offsets[k], en = s.offsets[k + 1];
+        pbf103::block_radix_stable(s.tmp + st, perm + st, en - st, 0xFFFFFFFFu, pbf103::radix_bits(n), sm, base,
+                                   tot);
+    }
 }
 
 __global__ void na_ranges(uint32_t C, Scratch s, uint32_t *__restrict__ cs, uint32_t *__restrict__ ce)
@@ -215,6 +241,7 @@ extern "C" pbf_status pbf_cell_sort_noalloc(const float *x_dev, uint32_t n, floa
     if (n) {
         na_scatter<<<(n + 255) / 256, 256, 0, st>>>(n, s);
         na_rank<<<(n + 255) / 256, 256, 0, st>>>(n, s, perm_dev);
+        if (n > kRankMax) na_big<<<kMaxBig, pbf103::kRadixThreads, 0, st>>>(n, s, perm_dev);
     }
     na_ranges<<<(C + 255) / 256, 256, 0, st>>>(C, s, cell_start_dev, cell_end_dev);
     e = cudaGetLastError();

@@ -8,9 +8,22 @@ on the machine that runs it (ref_build.build):
 
 Each fixture holds the seeded input, the parameters, and the reference's
 outputs: num, sorted positions/velocities, sorted hash and index arrays,
-cellStart/cellEnd and the neighbour list.  Before a scene is handed to the
-reference, the CPU oracle checks that it stays clear of three reference
-hazards: a particle with exactly 29 listed neighbours (opt::memorizeKernelCUDA
+cellStart/cellEnd and the neighbour list, per reference build:
+  ieee  the shipped counting-sort path, IEEE division and square root;
+  fast  the shipped fast-math flags (scenes without boundary contact);
+  cub   the reference's stable radix-sort path (-DUSE_CUB), whose sorted
+        index array is the permutation itself, bit for bit (scenes that
+        delete nothing: that path has no deletion).
+Fixtures whose name starts with "post_" run one_step's body with the
+post-solve passes the shipped step leaves commented out (XSPH, vorticity
+confinement; oracle/ref_driver.cu) and also hold the plain step's outputs
+(ieee0_*) for the velocity increments.  The "capped" fixture runs the cub
+build with no solver iteration at spacing h/2, where most particles reach
+the 29-neighbour cap: its lists pin the cap's selection order.
+
+Before a scene is handed to the reference, the CPU oracle checks that it
+stays clear of three reference hazards: a particle with exactly 29 listed
+neighbours in a scene that runs solver iterations (opt::memorizeKernelCUDA
 then reads into the next warp group's slots, pbf_kernel_memorization.cu:121-132),
 a delete cell id Gz*Gy*Gz-1 outside the table or occupied by a live particle
 (pbf_neighbor_search.cpp:146), and long collision loops (the reference's loop
@@ -73,7 +86,26 @@ def golden_cases():
     v = rng.normal(0, 2.0, size=x.shape).astype(np.float32)
     sc4 = scenes.Scene(x, v, (2.0, 2.0, 2.0), ((0.25, 0.25, 0.25), (1.8, 1.8, 1.8)), scenes.box_planes((2, 2, 2)))
     cases.append(("sparse_deletion", sc4, reflike(), "planes", 4))
+    # 7-9: the post-solve passes (ref_driver post modes 1-3) on the block of
+    # case 4 (random velocities: non-zero curl), with the reference dam's
+    # XSPH c (pbf_dam_init_cond.cpp:20) and a vorticity epsilon large enough
+    # that the confinement increment (h passed for 1/h shrinks it by h^8,
+    # pbf_vorticity_confinement.cu:28) stands far above rounding
+    pv = reflike(xsph_parameter=0.1, vc_parameter=VC_POST)
+    cases.append(("post_xsph", sc3, dict(pv, xsph_mode=1), "spheres", 4, 1))
+    cases.append(("post_vort_xsph", sc3, dict(pv, xsph_mode=1, vorticity_mode=1), "spheres", 4, 2))
+    cases.append(("post_vort", sc3, dict(pv, vorticity_mode=1), "spheres", 4, 3))
+    # 10: spacing h/2 (the benchmark configs' density), no solver iteration:
+    # interior particles meet ~30 candidates within h and keep the first 29
+    pc = reflike()
+    pc.update(smoothing_length=2 * s, cell_width=2 * s)
+    sc6 = scenes.dam_break(16, 16, 16, (2.0, 2.0, 2.0), scene_id=506, h=2 * s, spacing=s)
+    cases.append(("capped", sc6, pc, "planes", 0))
     return cases
+
+
+# vorticity epsilon of the post_* fixtures
+VC_POST = 2.0e4
 
 
 def boundary_arrays(sc, mode):
@@ -106,17 +138,18 @@ def check_hazards(sc, p, mode, iters):
     r = oracle_run(sc, p, mode, iters)
     live_keys = r["keys"][r["keys"] < C]
     assert not np.any(live_keys == delete_id), "a live particle sits in the reference's delete cell"
-    assert r["nnb"].max(initial=0) <= 28, "a particle reaches the 29-neighbour cap"
+    if iters > 0:  # the kernel-cache hazard runs only inside solver iterations
+        assert r["nnb"].max(initial=0) <= 28, "a particle reaches the 29-neighbour cap"
     assert 0 <= r["collision_passes"] <= 4, f"collision passes {r['collision_passes']}"
     assert sc.n % 32 == 0
     return r
 
 
-def write_input(path, sc, p, mode, iters, cap):
+def write_input(path, sc, p, mode, iters, cap, post=0):
     inner, outer, pts, nrm, use_b = boundary_arrays(sc, mode)
     with open(path, "wb") as f:
         f.write(b"PBFI")
-        f.write(struct.pack("<IIIii", 1, sc.n, cap, iters, use_b))
+        f.write(struct.pack("<IIIiii", 2, sc.n, cap, iters, use_b, post))
         f.write(np.array([p[k] for k in PARAM_ORDER], np.float32).tobytes())
         for a in (p["body_force"], sc.domain_end, sc.area[0], sc.area[1]):
             f.write(np.asarray(a, np.float32).reshape(3).tobytes())
@@ -149,41 +182,58 @@ def read_output(path):
     return out
 
 
-def main(out_dir):
+def main(out_dir, only=None):
     os.makedirs(out_dir, exist_ok=True)
-    exes = {v: ref_build.build(v) for v in ("ieee", "fast")}
-    for name, sc, p, mode, iters in golden_cases():
+    exes = {v: ref_build.build(v) for v in ("ieee", "fast", "cub")}
+    for case in golden_cases():
+        name, sc, p, mode, iters = case[:5]
+        post = case[5] if len(case) > 5 else 0
+        if only and name not in only:
+            continue
         p = dict(p)
         p["grid_size"] = list(api.calc_grid_size(2.0 * p["smoothing_length"], sc.domain_end))
         r = check_hazards(sc, p, mode, iters)
         cap = sc.n + 64
-        inp = os.path.join(out_dir, f"{name}.in.bin")
-        write_input(inp, sc, p, mode, iters, cap)
+        # (output key, build, post mode)
+        runs = [("ieee", "ieee", post)]
+        if post:
+            runs.append(("ieee0", "ieee", 0))  # the plain step: velocity increments of the post passes
+        else:
+            # the fast-math build only gets scenes with no boundary contact (one
+            # collision pass in the oracle), where its approximate division cannot
+            # change how the reference's unbounded collision loop ends
+            if r["collision_passes"] == 1 and iters > 0:
+                runs.append(("fast", "fast", 0))
+            if r["num"] == sc.n:  # the radix-sort path has no deletion
+                runs.append(("cub", "cub", 0))
         res = {}
-        # the fast-math build only gets scenes with no boundary contact (one
-        # collision pass in the oracle), where its approximate division cannot
-        # change how the reference's unbounded collision loop ends
-        variants = ["ieee", "fast"] if r["collision_passes"] == 1 else ["ieee"]
-        for v in variants:
-            exe = exes[v]
-            outp = os.path.join(out_dir, f"{name}.{v}.out.bin")
-            subprocess.run([exe, inp, outp], check=True, timeout=120)
-            res[v] = read_output(outp)
+        for key, build, pm in runs:
+            inp = os.path.join(out_dir, f"{name}.{key}.in.bin")
+            write_input(inp, sc, p, mode, iters, cap, pm)
+            outp = os.path.join(out_dir, f"{name}.{key}.out.bin")
+            subprocess.run([exes[build], inp, outp], check=True, timeout=120)
+            res[key] = read_output(outp)
             os.remove(outp)
-        os.remove(inp)
+            os.remove(inp)
         inner, outer, pts, nrm, use_b = boundary_arrays(sc, mode)
         arrays = {"x_in": sc.x, "v_in": sc.v, "inner": inner, "outer": outer, "plane_pts": pts,
                   "plane_nrm": nrm, "use_boundary": np.int32(use_b), "iters": np.int32(iters),
                   "domain_end": np.float32(sc.domain_end), "area_min": np.float32(sc.area[0]),
                   "area_max": np.float32(sc.area[1]),
                   "params": np.array([p[k] for k in PARAM_ORDER], np.float32),
-                  "body_force": np.float32(p["body_force"])}
+                  "body_force": np.float32(p["body_force"]), "post": np.int32(post),
+                  # some particle's list is cut at the cap: the kept set then
+                  # depends on the order inside a cell, which only the cub
+                  # build fixes
+                  "cap_binds": np.int32(int(r["nnb"].max(initial=0)) >= p["max_pair_particle_num"] - 1)}
         for v, r in res.items():
             for k, a in r.items():
                 arrays[f"{v}_{k}"] = np.asarray(a)
         np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), **arrays)
-        print(name, "num", res["ieee"]["num"], "of", sc.n)
+        print(name, "num", res["ieee"]["num"], "of", sc.n, "runs", [k for k, _, _ in runs])
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a[7:] for a in sys.argv[1:] if a.startswith("--only=")]
+    main(args[0] if args else os.path.dirname(os.path.abspath(__file__)), only or None)

@@ -135,6 +135,13 @@ def golden_case(path):
     p["body_force"] = [float(t) for t in fx["body_force"]]
     p["cell_width"] = p["smoothing_length"]
     p["grid_size"] = [int(t) for t in fx["ieee_grid"]]
+    # post-solve passes the fixture's reference run made (oracle/ref_driver.cu):
+    # 1 XSPH, 2 vorticity then XSPH, 3 vorticity; both in the reference's forms
+    post = int(fx["post"]) if "post" in fx else 0
+    if post in (1, 2):
+        p["xsph_mode"] = api.L.PBF_XSPH_WALK
+    if post in (2, 3):
+        p["vorticity_mode"] = api.L.PBF_VORTICITY_REFERENCE
     sc = scenes.Scene(fx["x_in"], fx["v_in"], tuple(float(t) for t in fx["domain_end"]),
                       (tuple(float(t) for t in fx["area_min"]), tuple(float(t) for t in fx["area_max"])),
                       (fx["plane_pts"], fx["plane_nrm"]))
@@ -158,6 +165,56 @@ def reference_of(fx, variant="ieee"):
     return {k[len(variant) + 1:]: fx[k] for k in fx if k.startswith(variant + "_")}
 
 
+def golden_with(variant):
+    """Fixture files holding outputs of a reference build ("cub") or run ("ieee0")."""
+    return [f for f in golden_files() if f"{variant}_num" in np.load(f).files]
+
+
+def compare_to_reference_exact(ours: dict, ref: dict) -> dict:
+    """Against the reference's stable radix-sort build (cub): the sorted
+    index array is the permutation, so every integer array is compared as
+    is, the neighbour lists slot by slot in their order (live particles'
+    entries; the reference fills only num * max_pair entries), and
+    positions and velocities in sorted order.  Returns the error report and
+    the number of mismatching integers per array."""
+    num = int(ref["num"])
+    assert ours["num"] == num, (ours["num"], num)
+    rep = {}
+    rep["perm"] = int(np.count_nonzero(np.asarray(ours["perm"])[:len(ref["sorted_index"])] != ref["sorted_index"]))
+    rep["sorted_hash"] = int(np.count_nonzero(np.asarray(ours["sorted_hash"])[:num] != ref["sorted_hash"][:num]))
+    cs_r, ce_r = ref["cell_start"], ref["cell_end"]
+    ne = cs_r != 0xFFFFFFFF
+    rep["cell_start"] = int(np.count_nonzero(np.asarray(ours["cell_start"]) != cs_r))
+    rep["cell_end"] = int(np.count_nonzero(np.asarray(ours["cell_end"])[ne] != ce_r[ne]))
+    mp = int(ref["max_pair"])
+    p = np.arange(num)
+    slots = ((np.arange(mp)[None, :] << 5) + ((p & 31) + ((p >> 5) << 5) * mp)[:, None]).reshape(-1)
+    nl_o, nl_r = np.asarray(ours["neighbor_list"])[slots], ref["neighbor_list"][slots]
+    rep["neighbor_list"] = int(np.count_nonzero(nl_o != nl_r))
+    rep["listed"] = int(np.count_nonzero(nl_r != 0xFFFFFFFF))
+    rep["pos_rel_err"] = pos_rel_err(ours["x"], ref["x"])
+    rep["vel_abs_err"] = float(np.abs(np.asarray(ours["v"], np.float64) - ref["v"]).max(initial=0))
+    return rep
+
+
+def by_id(v, perm, num):
+    """Rows of a sorted-order array placed by input index."""
+    out = np.zeros((len(perm), 3))
+    out[np.asarray(perm, np.int64)[:num]] = np.asarray(v, np.float64)[:num]
+    return out
+
+
+def post_increment_error(ours: dict, ours0: dict, ref: dict, ref0: dict) -> tuple:
+    """Velocity increments of the post-solve passes (run with them minus run
+    without), by particle id, ours against the reference's: (max error /
+    max reference increment, max reference increment)."""
+    num = int(ref["num"])
+    d_ref = by_id(ref["v"], ref["sorted_index"], num) - by_id(ref0["v"], ref0["sorted_index"], num)
+    d_our = by_id(ours["v"], ours["perm"], num) - by_id(ours0["v"], ours0["perm"], num)
+    scale = float(np.abs(d_ref).max(initial=0.0))
+    return float(np.abs(d_our - d_ref).max(initial=0.0)) / max(scale, 1e-30), scale
+
+
 def compare_to_reference(ours: dict, ref: dict, C: int) -> dict:
     """Compare a step's outputs with the reference's.  The reference's sort is
     a counting sort with atomic ranks, so the order inside a cell is
@@ -177,9 +234,10 @@ def compare_to_reference(ours: dict, ref: dict, C: int) -> dict:
     assert np.array_equal(ours["cell_start"][ne], cs_r[ne]) and np.array_equal(ours["cell_end"][ne], ce_r[ne])
     pr = ref["sorted_index"].astype(np.int64)
     po = np.asarray(ours["perm"]).astype(np.int64)
-    for c in np.nonzero(ne)[0]:
-        s, e = cs_r[c], ce_r[c]
-        assert np.array_equal(np.sort(pr[s:e]), np.sort(po[s:e])), c
+    # the same index set in every cell: order each cell's indices (the sorted
+    # hashes are equal, so (hash, index) order compares cell by cell)
+    sh = np.asarray(ref["sorted_hash"][:num], np.int64)
+    assert np.array_equal(pr[:num][np.lexsort((pr[:num], sh))], po[:num][np.lexsort((po[:num], sh))])
     assert np.array_equal(np.sort(pr[num:]), np.sort(po[num:]))
     # positions / velocities by particle id
     xr = np.zeros((len(pr), 3)); xo = np.zeros((len(pr), 3))
@@ -192,18 +250,17 @@ def compare_to_reference(ours: dict, ref: dict, C: int) -> dict:
     mp = int(ref["max_pair"])
 
     def sets(nl, perm):
-        out = {}
-        for p in range(num):
-            base = (p & 31) + ((p >> 5) << 5) * mp
-            ids = []
-            for k in range(mp):
-                q = nl[(k << 5) + base]
-                if q == 0xFFFFFFFF:
-                    break
-                ids.append(int(perm[q]))
-            out[int(perm[p])] = sorted(ids)
+        """Row id(p) holds the sorted ids of p's listed neighbours (-1 pads);
+        a list ends at its first empty slot."""
+        p = np.arange(num)
+        slots = (np.arange(mp)[None, :] << 5) + ((p & 31) + ((p >> 5) << 5) * mp)[:, None]
+        q = np.asarray(nl, np.int64)[slots]
+        live = np.cumprod(q != 0xFFFFFFFF, axis=1).astype(bool)
+        ids = np.where(live, perm[np.where(live, q, 0)], np.int64(-1))
+        out = np.full((len(perm), mp), -1, np.int64)
+        out[perm[:num]] = np.sort(ids, axis=1)
         return out
 
     so, sr = sets(np.asarray(ours["neighbor_list"]), po), sets(ref["neighbor_list"], pr)
-    rep["neighbor_set_mismatches"] = sum(1 for k in sr if sr[k] != so.get(k))
+    rep["neighbor_set_mismatches"] = int(np.count_nonzero((so != sr).any(axis=1)))
     return rep

@@ -2,9 +2,18 @@
 tests/golden/make_golden.py from the reference sources built for sm_103a).
 
 CPU part: the oracle reproduces the reference's outputs.  GPU part: the
-CUDA path reproduces them too.  Integers are compared on sort-invariant
-forms (the reference's counting sort orders a cell's particles by atomic
-arrival), positions within 1e-5 relative by particle id."""
+CUDA path reproduces them too.
+
+- The shipped counting-sort build ("ieee") orders a cell's particles by
+  atomic arrival, so its integers are compared on sort-invariant forms,
+  positions within 1e-5 relative by particle id.  Where the 29-neighbour cap
+  binds, the kept set depends on that arbitrary order and is not compared.
+- The stable radix-sort build ("cub", -DUSE_CUB) fixes the order: the
+  permutation, cell ranges and neighbour lists (in slot order, so the cap's
+  selection order too) are compared bit for bit.
+- post_* fixtures add the reference's XSPH and vorticity passes; their
+  velocity increments must agree within 1e-4 of the largest increment (the
+  FP32 and FP64 oracles agree on them to ~5e-6)."""
 import numpy as np
 import pytest
 
@@ -13,6 +22,13 @@ from tests import helpers as H
 FILES = H.golden_files()
 pytestmark = pytest.mark.skipif(not FILES, reason="no golden fixtures generated yet")
 IDS = [f.split("/")[-1][:-4] for f in FILES]
+CUB = H.golden_with("cub")
+CUB_IDS = [f.split("/")[-1][:-4] for f in CUB]
+POST = H.golden_with("ieee0")
+POST_IDS = [f.split("/")[-1][:-4] for f in POST]
+
+# post-pass velocity increments, relative to the largest increment
+POST_RTOL = 1e-4
 
 
 def oracle_outputs(O, sc, p, iters, fx, f64=False):
@@ -23,6 +39,25 @@ def oracle_outputs(O, sc, p, iters, fx, f64=False):
     return lay, C
 
 
+def gpu_outputs(sc, p, iters, fx):
+    from ssf_pbf_cuda_gb300 import api
+    part = api.PbfParticle(p, sc.n + 64, sc.domain_end)
+    part.set_particles(sc.x, sc.v)
+    api.one_step(part, H.golden_gpu_boundary(fx), sc.area, iters)
+    x, v = part.get_particles()
+    ours = part.neighbor_debug()
+    ours.update(x=x, v=v)
+    return ours
+
+
+def cap_binds(fx) -> bool:
+    return bool(int(fx["cap_binds"])) if "cap_binds" in fx else False
+
+
+def without_post(p):
+    return dict(p, xsph_mode=0, vorticity_mode=0)
+
+
 @pytest.mark.parametrize("path", FILES, ids=IDS)
 def test_oracle_matches_reference_ieee(oracle, path):
     sc, p, iters, fx = H.golden_case(path)
@@ -30,7 +65,8 @@ def test_oracle_matches_reference_ieee(oracle, path):
     for f64 in (False, True):
         ours, C = oracle_outputs(oracle, sc, p, iters, fx, f64)
         rep = H.compare_to_reference(ours, ref, C)
-        assert rep["neighbor_set_mismatches"] == 0
+        if not cap_binds(fx):
+            assert rep["neighbor_set_mismatches"] == 0
         assert rep["pos_rel_err"] <= H.POS_RTOL, rep
         assert rep["vel_abs_err"] <= H.vel_abs_tol(p["time_step"], ref["x"]), rep
 
@@ -47,19 +83,82 @@ def test_oracle_close_to_reference_fast_math(oracle, path):
     assert rep["pos_rel_err"] <= 1e-4, rep
 
 
+@pytest.mark.parametrize("path", CUB, ids=CUB_IDS)
+def test_oracle_matches_reference_stable_sort(oracle, path):
+    """Bit-exact permutation, cell ranges and ordered neighbour lists against
+    the reference's stable radix-sort build."""
+    sc, p, iters, fx = H.golden_case(path)
+    ref = H.reference_of(fx, "cub")
+    ours, _ = oracle_outputs(oracle, sc, p, iters, fx)
+    rep = H.compare_to_reference_exact(ours, ref)
+    for k in ("perm", "sorted_hash", "cell_start", "cell_end", "neighbor_list"):
+        assert rep[k] == 0, (k, rep)
+    assert rep["pos_rel_err"] <= H.POS_RTOL, rep
+    assert rep["vel_abs_err"] <= H.vel_abs_tol(p["time_step"], ref["x"]), rep
+
+
+def test_capped_fixture_binds_the_cap():
+    """The capped fixture is the one that pins the cap's selection order: most
+    of its particles keep 29 of more candidates within h."""
+    caps = [f for f in CUB if f.endswith("capped.npz")]
+    if not caps:
+        pytest.skip("no capped fixture")
+    fx = dict(np.load(caps[0]))
+    ref = H.reference_of(fx, "cub")
+    num, mp = int(ref["num"]), int(ref["max_pair"])
+    p = np.arange(num)
+    cnt = np.zeros(num, np.int64)
+    for k in range(mp):
+        cnt += ref["neighbor_list"][(k << 5) + (p & 31) + ((p >> 5) << 5) * mp] != 0xFFFFFFFF
+    assert (cnt == mp - 1).mean() > 0.5
+
+
+@pytest.mark.parametrize("path", POST, ids=POST_IDS)
+def test_oracle_post_passes_match_reference(oracle, path):
+    """XSPH and vorticity confinement as the reference computes them
+    (uncapped 27-cell walks, h passed for 1/h): velocity increments."""
+    sc, p, iters, fx = H.golden_case(path)
+    ref, ref0 = H.reference_of(fx, "ieee"), H.reference_of(fx, "ieee0")
+    ours, _ = oracle_outputs(oracle, sc, p, iters, fx)
+    ours0, _ = oracle_outputs(oracle, sc, without_post(p), iters, fx)
+    err, scale = H.post_increment_error(ours, ours0, ref, ref0)
+    assert scale > 1e-2, scale  # the fixture exercises the passes
+    assert err <= POST_RTOL, (err, scale)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", FILES, ids=IDS)
 def test_cuda_matches_reference(gpu, path):
-    from ssf_pbf_cuda_gb300 import api
     sc, p, iters, fx = H.golden_case(path)
     ref = H.reference_of(fx, "ieee")
-    part = api.PbfParticle(p, sc.n + 64, sc.domain_end)
-    part.set_particles(sc.x, sc.v)
-    api.one_step(part, H.golden_gpu_boundary(fx), sc.area, iters)
-    x, v = part.get_particles()
-    ours = part.neighbor_debug()
-    ours.update(x=x, v=v)
+    ours = gpu_outputs(sc, p, iters, fx)
     rep = H.compare_to_reference(ours, ref, int(np.prod(p["grid_size"])))
-    assert rep["neighbor_set_mismatches"] == 0
+    if not cap_binds(fx):
+        assert rep["neighbor_set_mismatches"] == 0
     assert rep["pos_rel_err"] <= H.POS_RTOL, rep
     assert rep["vel_abs_err"] <= H.vel_abs_tol(p["time_step"], ref["x"]), rep
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", CUB, ids=CUB_IDS)
+def test_cuda_matches_reference_stable_sort(gpu, path):
+    sc, p, iters, fx = H.golden_case(path)
+    ref = H.reference_of(fx, "cub")
+    rep = H.compare_to_reference_exact(gpu_outputs(sc, p, iters, fx), ref)
+    for k in ("perm", "sorted_hash", "cell_start", "cell_end", "neighbor_list"):
+        assert rep[k] == 0, (k, rep)
+    assert rep["pos_rel_err"] <= H.POS_RTOL, rep
+    assert rep["vel_abs_err"] <= H.vel_abs_tol(p["time_step"], ref["x"]), rep
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", POST, ids=POST_IDS)
+def test_cuda_post_passes_match_reference(gpu, path):
+    """The walk-form XSPH (PBF_XSPH_WALK) and reference-form vorticity
+    (PBF_VORTICITY_REFERENCE) kernels against the reference's own passes."""
+    sc, p, iters, fx = H.golden_case(path)
+    ref, ref0 = H.reference_of(fx, "ieee"), H.reference_of(fx, "ieee0")
+    err, scale = H.post_increment_error(gpu_outputs(sc, p, iters, fx), gpu_outputs(sc, without_post(p), iters, fx),
+                                        ref, ref0)
+    assert scale > 1e-2, scale
+    assert err <= POST_RTOL, (err, scale)

@@ -37,6 +37,45 @@ def test_config3_neighbour_search_bit_exact(oracle, gpu, kind):
     assert np.array_equal(np.sort(d["perm"]), np.arange(len(x), dtype=np.uint32))
 
 
+@pytest.mark.parametrize("n", [10000, 200000])
+def test_single_cell_pile_is_sorted_stably(oracle, gpu, n):
+    """Every particle in one cell.  The bucket's order is ascending input
+    index (the stable sort's) at any size, bit-exact against the oracle's
+    counting sort: 10,000 particles take the small-step path (ranked from
+    the particle side), 200,000 the large-step path (ranked per cell); both
+    hand the bucket to the block radix sort."""
+    rng = np.random.default_rng(n)
+    x = rng.uniform(0.31, 0.39, size=(n, 3)).astype(np.float32)
+    x[: n // 10] = rng.uniform(0.0, 0.8, size=(n // 10, 3))  # and a few other buckets
+    grid, cw = (8, 8, 8), 0.1
+    d = gpu_sort_only(x, grid, cw)
+    keys, perm, off = oracle.hash_sort(x, cw, grid)
+    assert int(np.diff(off[: 8 * 8 * 8 + 1]).max()) > 4096
+    assert np.array_equal(d["perm"], perm)
+    assert np.array_equal(d["sorted_hash"], keys[perm])
+
+
+@pytest.mark.parametrize("n", [50000, 300000])
+def test_mass_deletion_is_sorted_stably(oracle, gpu, n):
+    """A step that deletes about half its particles (far more than 4,096):
+    the deleted bucket, last in the order, is stable too, and the live count
+    and permutation equal the oracle's."""
+    rng = np.random.default_rng(77 + n)
+    x = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    grid, cw = (16, 16, 16), 0.1
+    amin, amax = (0.0, 0.0, 0.0), (0.5, 1.0, 1.0)
+    p = api.default_params(body_force=[0.0, 0.0, 0.0], grid_size=list(grid), cell_width=cw, smoothing_length=cw)
+    part = api.PbfParticle(p, n, (1.0, 1.0, 1.0))
+    part.set_particles(x, np.zeros_like(x))
+    api.one_step(part, None, (amin, amax), 0)
+    d = part.neighbor_debug()
+    keys, perm, off = oracle.hash_sort(x, cw, grid, amin, amax)
+    C = int(np.prod(grid))
+    assert n - int(off[C]) > 4096  # deleted
+    assert part.num == int(off[C])
+    assert np.array_equal(d["perm"], perm)
+
+
 def test_config2_single_large_step_properties(oracle, gpu):
     """1,048,576 particles, 2^21-cell table: the integer pipeline is bit-exact
     against the oracle and the permutation is a permutation."""

@@ -1,8 +1,12 @@
 """The reference's own CUDA step (yodaplusplus/ssf_pbf_cuda, built from its
 sources by oracle/ref_build.py) timed on this GPU beside the plain step of
-this library, on identical inputs and parameters.  Runs only where the
-reference's sources were prepared (oracle/_ref/src); scenes are checked
-against the reference's hazards first (tests/golden/make_golden.py)."""
+this library, on identical inputs and parameters, and its outputs compared
+with this library's at these sizes (32,768 and 1,048,576 particles): the
+reference's IEEE build's step against this library's step from the same
+input, as the golden fixtures are compared (sort-invariant integers,
+neighbour sets and positions by particle id, 1e-5 relative).  Runs only
+where the reference's sources were prepared (oracle/_ref/src); scenes are
+checked against the reference's hazards first (tests/golden/make_golden.py)."""
 import os
 import re
 import subprocess
@@ -12,6 +16,7 @@ import pytest
 
 from oracle import ref_build
 from ssf_pbf_cuda_gb300 import api, scenes
+from tests import helpers as H
 from tests.golden import make_golden as MG
 
 pytestmark = [pytest.mark.gpu,
@@ -40,8 +45,13 @@ def ref_exe():
     return ref_build.build("fast")  # the shipped flags
 
 
+@pytest.fixture(scope="module")
+def ref_exe_ieee():
+    return ref_build.build("ieee")  # IEEE division and square root: the parity build
+
+
 @pytest.mark.parametrize("name,make,grid", CASES, ids=[c[0] for c in CASES])
-def test_reference_gpu_step_time(tmp_path, gpu, ref_exe, name, make, grid):
+def test_reference_gpu_step_time(tmp_path, gpu, ref_exe, ref_exe_ieee, name, make, grid):
     import torch
     sc = make()
     p = ref_params(grid)
@@ -52,6 +62,8 @@ def test_reference_gpu_step_time(tmp_path, gpu, ref_exe, name, make, grid):
     MG.write_input(inp, sc, p, "planes", 4, sc.n)
     out = subprocess.run([ref_exe, inp, outp, str(REPS)], check=True, timeout=600, capture_output=True, text=True)
     ref_ms = float(re.search(r"ms_per_step ([0-9.eE+-]+)", out.stdout).group(1))
+    ref_fast = MG.read_output(outp)
+    subprocess.run([ref_exe_ieee, inp, outp], check=True, timeout=600)
     ref = MG.read_output(outp)
 
     dev = torch.device("cuda", 0)
@@ -72,8 +84,17 @@ def test_reference_gpu_step_time(tmp_path, gpu, ref_exe, name, make, grid):
     e1.record(stream)
     torch.cuda.synchronize()
     ours_ms = e0.elapsed_time(e1) / REPS
-    assert part.num == ref["num"]
+    assert part.num == ref["num"] == ref_fast["num"]
+    # the last timed step ran from the input: compare its outputs in full
+    x, v = part.get_particles()
+    ours = part.neighbor_debug()
+    ours.update(x=x, v=v)
+    rep = H.compare_to_reference(ours, ref, int(np.prod(p["grid_size"])))
     print(f"\n{name}: {sc.n} particles, 4 iterations: reference {ref_ms:.4f} ms/step "
           f"({sc.n / ref_ms / 1e3:.1f} M particle-steps/s), this library {ours_ms:.4f} ms/step "
-          f"({sc.n / ours_ms / 1e3:.1f} M particle-steps/s), {ref_ms / ours_ms:.2f}x")
+          f"({sc.n / ours_ms / 1e3:.1f} M particle-steps/s), {ref_ms / ours_ms:.2f}x; against the reference's "
+          f"outputs: {rep}")
+    assert rep["neighbor_set_mismatches"] == 0
+    assert rep["pos_rel_err"] <= H.POS_RTOL, rep
+    assert rep["vel_abs_err"] <= H.vel_abs_tol(p["time_step"], ref["x"]), rep
     assert ours_ms < ref_ms

@@ -111,3 +111,39 @@ def test_replicas_two_ranks_gloo():
     assert ms0 == ms1 == 11.0                # max over ranks
     assert tot0 == tot1 == n0 + n1           # whole-job particle count
     assert n0 == sum(s.n for s in replicas.rank_scenes(4, 0, 2))
+
+
+def test_oracle_side_params_equal_the_librarys(oracle, lib):
+    """The benchmark's CPU reference arm builds its parameters in oracle/params.py
+    so that it never loads the product library; they must be the library's
+    (pbf_params_init, config overrides, calcGridSize) field for field."""
+    from oracle import params as OP
+    from ssf_pbf_cuda_gb300 import api
+    a, b = OP.config_params(), api.config_params()
+    assert sorted(a) == sorted(b)
+    for k in a:
+        assert np.allclose(np.float32(a[k]), np.float32(b[k])), k
+    for sc in scenes.config4(12) + [scenes.config1(), scenes.config2()]:
+        p_lib = sc.params(api.config_params())
+        p_lib["grid_size"] = list(api.resolve_grid(p_lib, sc.domain_end))
+        assert OP.scene_params(sc)["grid_size"] == p_lib["grid_size"]
+
+
+def test_reference_arm_does_not_load_the_library(tmp_path):
+    """bench.py --impl reference runs the oracle only: after a (tiny) run the
+    process has no mapping of libpbf103.so."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import argparse, bench; "
+            "bench.run_reference(argparse.Namespace(scenes=2, steps=1, warmup=1, gpus=1)); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LIB' if 'libpbf103' in maps else 'CLEAN', 'ORACLE' if 'libpbf_oracle' in maps else '')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600,
+                         env=dict(os.environ, OMP_NUM_THREADS="2"))
+    assert out.returncode == 0, out.stderr[-2000:]
+    last = out.stdout.strip().splitlines()[-1]
+    assert last.split() == ["CLEAN", "ORACLE"], out.stdout[-2000:]
+    import json
+    line = json.loads(out.stdout.strip().splitlines()[-2])
+    assert line["impl"] == "reference" and line["config"]["particles_per_gpu"] > 0

@@ -49,9 +49,12 @@ def noalloc_sort(lib, x, grid, cw):
 
 def test_noalloc_sort_matches_allocating_path_twice(lib, gpu):
     rng = np.random.default_rng(2026)
+    pile = rng.uniform(0.0, 1.6, size=(60000, 3)).astype(np.float32)
+    pile[:30000] = rng.uniform(0.81, 0.89, size=(30000, 3))  # one bucket of 30,000 (> 4,096) entries
     cases = [
         (rng.uniform(-0.2, 1.8, size=(20000, 3)).astype(np.float32), (16, 16, 8), 0.1),
         (rng.normal(0.6, 0.2, size=(7777, 3)).astype(np.float32), (32, 16, 16), 0.07),
+        (pile, (16, 16, 16), 0.1),
     ]
     for x, grid, cw in cases:  # two calls in a row on the shared scratch
         want = allocating_sort(x, grid, cw)
