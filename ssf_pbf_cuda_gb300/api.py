@@ -519,6 +519,14 @@ class Batch:
         check(load().pbf_batch_set_all(self.handle, c.ctypes.data if c is not None else None, _ptr(x), _ptr(v),
                                        1 if dev else 0, _stream(stream)), "pbf_batch_set_all")
 
+    def live_counts(self, stream=None) -> np.ndarray:
+        """Live particles of every active scene (scene-id order); waits for the stream."""
+        n = len(self.scene_ids())
+        counts = np.zeros(max(n, 1), np.uint32)
+        check(load().pbf_batch_get_all(self.handle, counts.ctypes.data, None, None, 0, _stream(stream)),
+              "pbf_batch_get_all")
+        return counts[:n]
+
     def get_all(self, x_out=None, v_out=None, stream=None):
         """Download every active scene into packed buffers; returns counts.
         With x_out None, numpy arrays are allocated and returned as (counts, x, v)."""

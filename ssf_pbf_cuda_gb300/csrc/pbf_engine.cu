@@ -149,6 +149,11 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
     d->inv_wdq = wdq > 0.f ? 1.f / wdq : 0.f;
     d->scorr_k = p.scorr_k;
     d->scorr_n = p.scorr_n;
+    // the pair passes evaluate s_corr as a constant times a power of W:
+    // 10 W^4 / W(0.4h)^4 and k (W / W(dq h))^n = (k / W(dq h)^n) W^n
+    d->ih2 = inv_h2;
+    d->tens_c = 10.f * d->inv_k;
+    d->scorr_c = (float)((double)p.scorr_k * std::pow((double)d->inv_wdq, p.scorr_n));
     d->tensile_mode = p.tensile_mode;
     d->xsph_mode = p.xsph_mode;
     d->vort_mode = p.vorticity_mode;

@@ -105,6 +105,11 @@ public:
     int device() const { return device_; }
     uint64_t arena_bytes() const { return arena_bytes_; }
     bool can_fit(uint32_t capacity, uint64_t cells, uint64_t bnd_len) const;
+    // whether a scene of this size fits the empty arena at all
+    bool ever_fits(uint32_t capacity, uint64_t cells) const
+    {
+        return capacity <= max_particles_ && cells <= max_cells_;
+    }
 
 private:
     pbf_status upload(cudaStream_t st);

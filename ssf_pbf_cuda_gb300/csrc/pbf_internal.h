@@ -49,7 +49,9 @@ struct SceneDesc {
     uint32_t n_outer;
     uint32_t n_planes;
     uint32_t builtin_sphere;
-    uint32_t pad0, pad1, pad2;
+    float ih2;           // 1/h^2 (poly6 from r^2)
+    float tens_c;        // reference s_corr: 10 / W(0.4h)^4, the factor of W^4
+    float scorr_c;       // textbook s_corr: k / W(dq h)^n, the factor of W^n
 };
 static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
 

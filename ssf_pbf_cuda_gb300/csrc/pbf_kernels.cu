@@ -64,58 +64,77 @@ __device__ __forceinline__ float dist2_exact(float4 a, float4 b)
     return __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
 }
 
-// Kernel value and gradient for a listed pair at current positions:
-// memorizeKernelPair, src/pbf/solver/cuda/pbf_kernel_memorization.cu:14-56.
-// Every product and sum is explicitly rounded (no contraction left to the
-// compiler), here and in the sums below, so that the one-lane passes and the
-// split passes of small steps give the same bits.
-struct PairK {
-    float W;
-    float gx, gy, gz;
+// A listed pair at current positions (memorizeKernelPair,
+// src/pbf/solver/cuda/pbf_kernel_memorization.cu:14-56, restated): the
+// difference d = x_i - x_j, r^2, the poly6 value W and the spiky gradient
+// as a factor s of d (grad W = s d):
+//   W = alpha (1 - r^2 / h^2)^3          for r <= h, else 0
+//   s = beta (1 - r / h)^2 / r           for 0 < r <= h, else 0
+//   sr = s r = |grad W| (up to sign)
+// The clamps replace the reference's branches: 1 - r^2/h^2 and 1 - r/h are
+// clamped at 0 (r > h), and r^2 enters the reciprocal square root no smaller
+// than kMinR2, so the pair of a particle with itself (r^2 = 0, d = 0, r = 0)
+// gets a finite s (up to beta / 1e-15), a gradient s d of exactly 0 and
+// sr = 0, as the reference's r^2 > 0 test gives.  |grad W|^2 is taken as
+// sr^2, not s^2 r^2: the latter overflows for the self pair.
+// Products and sums are rounded one by one or fused where written
+// (__fmaf_rn), never contracted by the compiler, so every pass that calls
+// these, in one lane or split over lanes, gets the same bits.
+constexpr float kMinR2 = 1e-30f;
+
+struct PairGeo {
+    float d0, d1, d2, r2;
 };
 
-__device__ __forceinline__ PairK pair_kernel(float4 xi, float4 xj, float inv_h, float alpha, float beta)
+__device__ __forceinline__ PairGeo pair_geo(float4 xi, float4 xj)
 {
-    PairK o;
-    const float d0 = __fsub_rn(xi.x, xj.x), d1 = __fsub_rn(xi.y, xj.y), d2 = __fsub_rn(xi.z, xj.z);
-    const float r2 = __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
-    const float inv_r = rsqrtf(r2);
-    const float q2 = __fmul_rn(__fmul_rn(r2, inv_h), inv_h);
-    o.W = 0.f;
-    if (q2 <= 1.f) {
-        const float t = __fsub_rn(1.f, q2);
-        o.W = __fmul_rn(__fmul_rn(__fmul_rn(alpha, t), t), t);
-    }
-    const float r = __fmul_rn(r2, inv_r);
-    const float u = __fmaf_rn(-r, inv_h, 1.f);
-    const float kd = (inv_h <= inv_r) ? __fmul_rn(__fmul_rn(beta, u), u) : 0.f;
-    // grad W = 0 for the pair with itself (r2 = 0, where kd and inv_r are not finite)
-    const float s = (r2 > 0.f) ? __fmul_rn(kd, inv_r) : 0.f;
-    o.gx = __fmul_rn(s, d0);
-    o.gy = __fmul_rn(s, d1);
-    o.gz = __fmul_rn(s, d2);
-    return o;
+    PairGeo g;
+    g.d0 = __fsub_rn(xi.x, xj.x);
+    g.d1 = __fsub_rn(xi.y, xj.y);
+    g.d2 = __fsub_rn(xi.z, xj.z);
+    g.r2 = __fmaf_rn(g.d2, g.d2, __fmaf_rn(g.d1, g.d1, __fmul_rn(g.d0, g.d0)));
+    return g;
 }
 
-// |grad W|^2 of a pair, in the order calcScalingFactor sums it (z, y, x).
-__device__ __forceinline__ float grad2(const PairK &p)
+struct PairWS {
+    float W, s, sr;
+};
+
+// per-scene constants of the pair math, in registers for a particle's loop
+struct PairConst {
+    float ih2, inv_h, alpha, beta;
+};
+
+__device__ __forceinline__ PairConst pair_const(const SceneDesc &d)
 {
-    return __fmaf_rn(p.gz, p.gz, __fmaf_rn(p.gy, p.gy, __fmul_rn(p.gx, p.gx)));
+    return PairConst{d.ih2, d.inv_h, d.alpha, d.beta};
+}
+
+__device__ __forceinline__ PairWS pair_ws(float r2, const PairConst &c)
+{
+    const float inv_r = rsqrtf(fmaxf(r2, kMinR2));
+    const float t = fmaxf(__fmaf_rn(-r2, c.ih2, 1.f), 0.f);
+    const float W = __fmul_rn(__fmul_rn(c.alpha, t), __fmul_rn(t, t));
+    const float r = __fmul_rn(r2, inv_r);
+    const float u = fmaxf(__fmaf_rn(-r, c.inv_h, 1.f), 0.f);
+    const float s = __fmul_rn(__fmul_rn(c.beta, inv_r), __fmul_rn(u, u));
+    return PairWS{W, s, __fmul_rn(s, r)};
 }
 
 // The sums of calcScalingFactorCUDA (pbf_constraint.cu:168-209) over a
-// particle's list, added in list order.
+// particle's list, added in list order: sum W, sum grad W = sum s d, and
+// sum |grad W|^2 = sum (s r)^2.
 struct LamSum {
     float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
-    __device__ __forceinline__ void add(float W, float gx, float gy, float gz, float k2)
+    __device__ __forceinline__ void add(float W, float s, float d0, float d1, float d2, float sr)
     {
         ks = __fadd_rn(ks, W);
-        g0 = __fadd_rn(g0, gx);
-        g1 = __fadd_rn(g1, gy);
-        g2 = __fadd_rn(g2, gz);
-        kg2 = __fadd_rn(kg2, k2);
+        g0 = __fmaf_rn(s, d0, g0);
+        g1 = __fmaf_rn(s, d1, g1);
+        g2 = __fmaf_rn(s, d2, g2);
+        kg2 = __fmaf_rn(sr, sr, kg2);
     }
-    __device__ __forceinline__ void add(const PairK &p) { add(p.W, p.gx, p.gy, p.gz, grad2(p)); }
+    __device__ __forceinline__ void add(const PairGeo &g, const PairWS &k) { add(k.W, k.s, g.d0, g.d1, g.d2, k.sr); }
     // lambda = C / (m^2 / rho0^2 |grad C|^2 + eps)
     __device__ __forceinline__ float lambda(const SceneDesc &d) const
     {
@@ -124,6 +143,13 @@ struct LamSum {
         return __fdiv_rn(C, __fmaf_rn(d.m2rho2, K, d.relax));
     }
 };
+
+// one listed pair's terms of the lambda sums
+__device__ __forceinline__ void lam_add(LamSum &ls, float4 xi, float4 xj, const PairConst &c)
+{
+    const PairGeo g = pair_geo(xi, xj);
+    ls.add(g, pair_ws(g.r2, c));
+}
 
 // WspikyDerivative, src/pbf/kernel/cuda/detail/pbf_kernel.inl:48-63.
 __device__ __forceinline__ float wspiky_d(float r, float kinv_h)
@@ -142,8 +168,8 @@ __device__ __forceinline__ void inner_sphere(bool &hit, float3 &dp, float3 p, fl
 {
     const float c0 = s.x - p.x, c1 = s.y - p.y, c2 = s.z - p.z;
     const float d2 = fmaf(c2, c2, fmaf(c1, c1, c0 * c0));
-    const float rinv = rsqrtf(d2);
     if (d2 > s.w * s.w) {
+        const float rinv = rsqrtf(d2);
         hit = true;
         dp.x = fmaf(c0, 1.0001f, dp.x);
         dp.y = fmaf(c1, 1.0001f, dp.y);
@@ -154,13 +180,17 @@ __device__ __forceinline__ void inner_sphere(bool &hit, float3 &dp, float3 p, fl
     }
 }
 
-// responsePlaneBoundary, src/pbf/solver/cuda/boundary/pbf_plane_boundary.cu:6-45
+// responsePlaneBoundary, src/pbf/solver/cuda/boundary/pbf_plane_boundary.cu:6-45.
+// Both of its hit cases need the projected point p behind the plane
+// ((p - on) . n < 0); that is tested first, so a particle clear of the plane
+// (the common case) skips the rest, with the same result.
 __device__ __forceinline__ void plane(bool &hit, float3 &dp, float3 o, float3 p, float4 on, float4 n)
 {
-    const float pa0 = o.x - on.x, pa1 = o.y - on.y, pa2 = o.z - on.z;
     const float pb0 = p.x - on.x, pb1 = p.y - on.y, pb2 = p.z - on.z;
-    const float pa_n = fmaf(pa2, n.z, fmaf(pa1, n.y, pa0 * n.x));
     const float pb_n = fmaf(pb2, n.z, fmaf(pb1, n.y, pb0 * n.x));
+    if (!(pb_n < 0.f)) return;
+    const float pa0 = o.x - on.x, pa1 = o.y - on.y, pa2 = o.z - on.z;
+    const float pa_n = fmaf(pa2, n.z, fmaf(pa1, n.y, pa0 * n.x));
     float3 is;
     if (pa_n == 0.f && pb_n == 0.f) {
         return;
@@ -1013,7 +1043,8 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     const uint32_t i = d.p_off + local;
     const uint32_t shift = d.p_off - base;
     const float4 xp = a.xa[i];
-    const float h2 = d.h2, inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const float h2 = d.h2;
+    const PairConst pc = pair_const(d);
     const uint32_t cap = d.cap;
     const uint64_t stride = a.nbr_stride;
     uint32_t *nl = list_of(a.nbr, i);
@@ -1022,8 +1053,11 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // phase 1: the walk only tests and records (lanes of a warp accept
     // different candidates, so pair math inside the walk would run masked
     // for almost every candidate); a candidate's .w is its sorted slot
-    // Candidates are fetched kNbFetch at a time (more loads in flight) and
-    // tested in order, so the first `cap` accepted ones are the reference's.
+    // Candidates are fetched kNbFetch at a time (more loads in flight; a
+    // group past the range's end re-reads its last candidate), all of the
+    // group is tested first (independent chains), then the accepted ones are
+    // appended in order up to the cap, so the first `cap` accepted ones are
+    // the reference's.
     constexpr uint32_t kNbFetch = 4;
     uint32_t cnt = 0;
     walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
@@ -1031,18 +1065,21 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
             float4 c[kNbFetch];
 #pragma unroll
-            for (uint32_t k = 0; k < kNbFetch; ++k)
-                if (q0 + k < en) c[k] = __ldg(src + q0 + k);
+            for (uint32_t k = 0; k < kNbFetch; ++k) c[k] = __ldg(src + min(q0 + k, en - 1u));
+            bool acc[kNbFetch];
+#pragma unroll
+            for (uint32_t k = 0; k < kNbFetch; ++k) acc[k] = (q0 + k < en) && dist2_exact(xp, c[k]) < h2;
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) {
-                if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
+                if (acc[k] && cnt < cap) {
                     if (SMEM)
                         s_list[cnt * blockDim.x + threadIdx.x] = __float_as_uint(c[k].w);
                     else
                         nl[list_slot(cnt, stride)] = __float_as_uint(c[k].w);
-                    if (++cnt == cap) return false;
+                    ++cnt;
                 }
             }
+            if (cnt == cap) return false;
         }
         return true;
     });
@@ -1065,13 +1102,13 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
         for (uint32_t k = 0; k < cnt; ++k) {
             const uint32_t q = *rd;
             rd += blockDim.x;
-            ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
+            lam_add(ls, xp, __ldg(xa + q), pc);
         }
     } else {
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
             const uint32_t q = nl[list_slot(k, stride)];
-            ls.add(pair_kernel(xp, __ldg(xa + q), inv_h, alpha, beta));
+            lam_add(ls, xp, __ldg(xa + q), pc);
         }
     }
     a.lam[i] = ls.lambda(d);
@@ -1119,24 +1156,26 @@ __device__ __forceinline__ LamSum lam_sum_split(const uint32_t *nl, uint64_t str
                                                 const float4 *__restrict__ xc, float4 xp, const SceneDesc &d,
                                                 uint32_t sub, uint32_t gmask)
 {
-    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const PairConst pc = pair_const(d);
     LamSum ls;
     float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub));
     uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit);
     for (uint32_t k0 = 0; k0 < nn; k0 += kSplit) {
         const float4 x1 = __ldg(xc + q1);
         q1 = split_index<RO>(nl, stride, nn, k0 + 2 * kSplit + sub);
-        PairK pk{0.f, 0.f, 0.f, 0.f};
-        if (k0 + sub < nn) pk = pair_kernel(xp, x0, inv_h, alpha, beta);
-        const float k2 = grad2(pk);
+        // this lane's pair (slot k0 + sub); a slot past the list reads
+        // index 0 and is not added
+        const PairGeo g = pair_geo(xp, x0);
+        const PairWS k = pair_ws(g.r2, pc);
 #pragma unroll
         for (uint32_t j = 0; j < kSplit; ++j) {
-            const float W = __shfl_sync(gmask, pk.W, j, kSplit);
-            const float gx = __shfl_sync(gmask, pk.gx, j, kSplit);
-            const float gy = __shfl_sync(gmask, pk.gy, j, kSplit);
-            const float gz = __shfl_sync(gmask, pk.gz, j, kSplit);
-            const float kk = __shfl_sync(gmask, k2, j, kSplit);
-            if (k0 + j < nn) ls.add(W, gx, gy, gz, kk);
+            const float W = __shfl_sync(gmask, k.W, j, kSplit);
+            const float s = __shfl_sync(gmask, k.s, j, kSplit);
+            const float d0 = __shfl_sync(gmask, g.d0, j, kSplit);
+            const float d1 = __shfl_sync(gmask, g.d1, j, kSplit);
+            const float d2 = __shfl_sync(gmask, g.d2, j, kSplit);
+            const float sr = __shfl_sync(gmask, k.sr, j, kSplit);
+            if (k0 + j < nn) ls.add(W, s, d0, d1, d2, sr);
         }
         x0 = x1;
     }
@@ -1191,15 +1230,18 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
                 for (uint32_t q0 = st; q0 < en; q0 += 4) {
                     float4 c[4];
 #pragma unroll
-                    for (uint32_t k = 0; k < 4; ++k)
-                        if (q0 + k < en) c[k] = __ldg(src + q0 + k);
+                    for (uint32_t k = 0; k < 4; ++k) c[k] = __ldg(src + min(q0 + k, en - 1u));
+                    bool acc[4];
+#pragma unroll
+                    for (uint32_t k = 0; k < 4; ++k) acc[k] = (q0 + k < en) && dist2_exact(xp, c[k]) < h2;
 #pragma unroll
                     for (uint32_t k = 0; k < 4; ++k) {
-                        if (q0 + k < en && dist2_exact(xp, c[k]) < h2) {
+                        if (acc[k] && cnt < cap) {
                             buf[cnt] = __float_as_uint(c[k].w);
-                            if (++cnt == cap) return false;
+                            ++cnt;
                         }
                     }
+                    if (cnt == cap) return false;
                 }
                 return true;
             }, rr0, rr1);
@@ -1240,11 +1282,11 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
     const uint32_t i = d.p_off + local;
-    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const PairConst pc = pair_const(d);
     const float4 xp = xc[i];
     LamSum ls;
     list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i],
-                      [&](uint32_t q) { ls.add(pair_kernel(xp, __ldg(xc + q), inv_h, alpha, beta)); });
+                      [&](uint32_t q) { lam_add(ls, xp, __ldg(xc + q), pc); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
     // delta-p pass gathers next (neighbours here use only .xyz); small,
     // latency-bound steps keep it in its own array, as the store into the
@@ -1262,29 +1304,31 @@ enum ScorrForm { kScorrReference, kScorrTextbook, kScorrOff, kScorrTextbook4 };
 
 struct ScorrConst {
     float sci;  // max(-lambda_i, 0), the reference form's own share
-    float inv_k, inv_wdq, sk;
+    float c;    // the factor of W^n: 10 / W(0.4h)^4 (reference), k / W(dq h)^n (textbook)
     int sn;
 };
 
 // -(lambda_i + lambda_j + s_corr) for a pair (the coefficient of grad W in
-// calcPositionUpdateCUDA, pbf_position_update.cu:131-188), with s_corr's last
-// product fused into the sum.
+// calcPositionUpdateCUDA, pbf_position_update.cu:131-188).  s_corr as a
+// constant times a power of W: reference 10 W^4 / W(0.4h)^4 (max(-lambda_i,
+// 0) + max(-lambda_j, 0)) (pbf_position_update.cu:136-146), textbook
+// k (W / W(dq h))^n (Macklin and Mueller 2013, eq. 13); its last product is
+// fused into the sum.
 template <int FORM>
 __device__ __forceinline__ float dp_coef(float li, float lj, float W, const ScorrConst &c)
 {
     const float ll = __fadd_rn(li, lj);
     if (FORM == kScorrReference) {
-        const float kr2 = __fmul_rn(W, W);
-        const float tc = __fmul_rn(__fmul_rn(10.f, __fmul_rn(kr2, kr2)), c.inv_k);
-        return -__fmaf_rn(__fadd_rn(c.sci, (lj < 0.f) ? -lj : 0.f), tc, ll);
-    } else if (FORM == kScorrTextbook4) {  // the loop below for n = 4, same products in the same order
-        const float ratio = __fmul_rn(W, c.inv_wdq);
-        return -__fmaf_rn(c.sk, __fmul_rn(__fmul_rn(__fmul_rn(ratio, ratio), ratio), ratio), ll);
+        const float w2 = __fmul_rn(W, W);
+        const float tc = __fmul_rn(c.c, __fmul_rn(w2, w2));
+        return -__fmaf_rn(__fadd_rn(c.sci, fmaxf(-lj, 0.f)), tc, ll);
+    } else if (FORM == kScorrTextbook4) {
+        const float w2 = __fmul_rn(W, W);
+        return -__fmaf_rn(c.c, __fmul_rn(w2, w2), ll);
     } else if (FORM == kScorrTextbook) {
-        const float ratio = __fmul_rn(W, c.inv_wdq);
         float pw = 1.f;
-        for (int e = 0; e < c.sn; ++e) pw = __fmul_rn(pw, ratio);
-        return -__fmaf_rn(c.sk, pw, ll);
+        for (int e = 0; e < c.sn; ++e) pw = __fmul_rn(pw, W);
+        return -__fmaf_rn(c.c, pw, ll);
     }
     return -ll;
 }
@@ -1292,32 +1336,32 @@ __device__ __forceinline__ float dp_coef(float li, float lj, float W, const Scor
 __device__ __forceinline__ ScorrConst scorr_const(const SceneDesc &d, float li)
 {
     ScorrConst c;
-    c.sci = (li < 0.f) ? -li : 0.f;
-    c.inv_k = d.inv_k;
-    c.inv_wdq = d.inv_wdq;
-    c.sk = d.scorr_k;
+    c.sci = fmaxf(-li, 0.f);
+    c.c = d.tensile_mode == PBF_TENSILE_REFERENCE ? d.tens_c : d.scorr_c;
     c.sn = d.scorr_n;
     return c;
 }
 
 // Sum over the list of -(lambda_i + lambda_j + s_corr) grad W (the body of
-// calcPositionUpdateCUDA, pbf_position_update.cu:131-188), in list order.
+// calcPositionUpdateCUDA, pbf_position_update.cu:131-188), in list order:
+// each pair adds (coefficient * s) d.
 template <int kChunk, int FORM, bool LAMW>
 __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, const float4 *__restrict__ xc,
                                          uint32_t i, float4 xp, float li)
 {
-    const float inv_h = d.inv_h, alpha = d.alpha, beta = d.beta;
+    const PairConst pc = pair_const(d);
     const ScorrConst sc = scorr_const(d, li);
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], [&](uint32_t q) {
         const float4 xq = __ldg(xc + q);
-        const PairK pk = pair_kernel(xp, xq, inv_h, alpha, beta);
+        const PairGeo g = pair_geo(xp, xq);
+        const PairWS k = pair_ws(g.r2, pc);
         const float lj = LAMW ? xq.w : __ldg(lam + q);  // LAMW: lambda in .w of the positions
-        const float cc = dp_coef<FORM>(li, lj, pk.W, sc);
-        s0 = __fmaf_rn(cc, pk.gx, s0);
-        s1 = __fmaf_rn(cc, pk.gy, s1);
-        s2 = __fmaf_rn(cc, pk.gz, s2);
+        const float f = __fmul_rn(dp_coef<FORM>(li, lj, k.W, sc), k.s);
+        s0 = __fmaf_rn(f, g.d0, s0);
+        s1 = __fmaf_rn(f, g.d1, s1);
+        s2 = __fmaf_rn(f, g.d2, s2);
     });
     return make_float3(s0, s1, s2);
 }

@@ -91,20 +91,20 @@ pbf_status pbf_server::service(bool *did_work)
         const uint32_t cap = r->desc.capacity ? r->desc.capacity : r->n;
         pbf_status rc = batch.add_scene(r->desc.params, cap, de, r->bnd.get(), r->desc.area_min, r->desc.area_max,
                                         r->x.data(), r->v.data(), r->n, false, stream, &id);
-        if (rc == PBF_ERROR_OUT_OF_MEMORY || rc == PBF_ERROR_CAPACITY) {
+        std::lock_guard<std::mutex> lk(mu);
+        if ((rc == PBF_ERROR_OUT_OF_MEMORY || rc == PBF_ERROR_CAPACITY) && !resident.empty()) {
             // arena full or fragmented: retry after the next eviction
-            std::lock_guard<std::mutex> lk(mu);
             queue.push_front(r->id);
             break;
         }
-        std::lock_guard<std::mutex> lk(mu);
-        if (rc != PBF_SUCCESS) {
+        if (rc != PBF_SUCCESS) {  // refused, or too large even for the arena with nothing resident
             r->done = true;
             r->complete = now();
             r->flags = 0xFFFFFFFFu;
             st.rejected++;
             pbf_completion c{r->id, 0, 0, r->flags, r->arrival, r->complete, r->complete};
             completions.push_back(c);
+            *did_work = true;
             continue;
         }
         r->scene = id;
@@ -234,6 +234,10 @@ pbf_status pbf_server_submit(pbf_server *s, const pbf_request_desc *req, const f
     uint64_t bytes = 0;
     pbf_status rc = pbf_scene_bytes(&req->params, cap, req->domain_end, &bytes);
     if (rc != PBF_SUCCESS) return rc;
+    SceneDesc d;
+    uint32_t grid[3];
+    rc = derive_desc(req->params, req->domain_end, &d, grid);
+    if (rc != PBF_SUCCESS) return rc;
     std::unique_ptr<Request> r(new (std::nothrow) Request());
     if (!r) return PBF_ERROR_OUT_OF_MEMORY;
     r->desc = *req;
@@ -254,6 +258,12 @@ pbf_status pbf_server_submit(pbf_server *s, const pbf_request_desc *req, const f
     if (bytes > s->cfg.hbm_budget_bytes) {
         s->st.rejected++;
         return PBF_ERROR_BUDGET;
+    }
+    // a request larger than the empty arena would wait forever at the head of
+    // the queue: refuse it here
+    if (!s->batch.ever_fits(cap, (uint64_t)d.ncell + 1)) {
+        s->st.rejected++;
+        return PBF_ERROR_CAPACITY;
     }
     r->id = s->next_id++;
     r->arrival = s->now();

@@ -311,3 +311,34 @@ def test_server_threaded_loop_with_live_arrivals(gpu):
     assert done == set(rids)
     for (sc, p, hz), rid in zip(reqs, rids):
         assert np.array_equal(srv.result(rid)[0], alone(sc, p, hz)["x"])
+
+
+def test_server_refuses_requests_larger_than_the_arena(gpu):
+    """A request whose particles or cells exceed the empty arena can never be
+    admitted: submit refuses it (PBF_ERROR_CAPACITY) instead of queueing it
+    at the head forever, and requests behind it are served."""
+    import threading
+    reqs = server_requests(2)
+    (sc, p, hz), (sc2, p2, hz2) = reqs
+    srv = api.Server(hbm_budget_bytes=1 << 34, max_scenes=4, max_particles=sc.n - 1, max_cells=200000, iters=4)
+    with pytest.raises(pbf.PbfError) as e:
+        srv.submit(H.resolved(p, sc), sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes)
+    assert e.value.status == 4
+    cells = int(np.prod(H.resolved(p, sc)["grid_size"]))
+    srv2 = api.Server(hbm_budget_bytes=1 << 34, max_scenes=4, max_particles=20000, max_cells=cells, iters=4)
+    with pytest.raises(pbf.PbfError) as e:  # the scene needs cells + 1 (its deleted bucket)
+        srv2.submit(H.resolved(p, sc), sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes)
+    assert e.value.status == 4
+    srv3 = api.Server(hbm_budget_bytes=1 << 34, max_scenes=4, max_particles=sc2.n, max_cells=200000, iters=4)
+    srv3.start()
+    if sc.n > sc2.n:
+        with pytest.raises(pbf.PbfError):
+            srv3.submit(H.resolved(p, sc), sc.domain_end, sc.area, sc.x, sc.v, horizon_steps=hz, planes=sc.planes)
+    rid = srv3.submit(H.resolved(p2, sc2), sc2.domain_end, sc2.area, sc2.x, sc2.v, horizon_steps=hz2,
+                      planes=sc2.planes)
+    t = threading.Thread(target=srv3.stop, kwargs={"drain": True})
+    t.start()
+    t.join(timeout=120)
+    assert not t.is_alive()
+    assert {c["request_id"] for c in srv3.poll()} == {rid}
+    assert np.array_equal(srv3.result(rid)[0], alone(sc2, p2, hz2)["x"])

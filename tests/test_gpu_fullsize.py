@@ -87,50 +87,59 @@ def test_config2_single_large_step_properties(oracle, gpu):
     assert np.array_equal(np.sort(g["perm"]), np.arange(sc.n, dtype=np.uint32))
 
 
-def test_long_run_statistics_match_fp64_oracle(oracle, gpu):
-    """A 60-step dam break with stable parameters (64 neighbour slots, s_corr
-    k = 1e-4): mean density error and kinetic energy of the GPU run stay
-    within 1% of the FP64 oracle run from the same start, or, where FP32
-    rounding alone moves the statistic further than that, no further from
-    FP64 than twice the FP32 oracle's own distance (the trajectories are
-    chaotic: after 60 steps any FP32 implementation has left the FP64 one)."""
-    sc = scenes.dam_break(16, 16, 16, (2.0, 1.5, 1.5), scene_id=77)
+def _kinetic(p, v):
+    return 0.5 * p["particle_mass"] * float((np.asarray(v, np.float64) ** 2).sum())
+
+
+def _mean_density_error(oracle, p, x):
+    """Mean |rho / rho0 - 1| with each particle's neighbour list from the
+    oracle (a step of 0 iterations on x, FP64), W summed in FP64."""
+    m, h = p["particle_mass"], p["smoothing_length"]
+    rr = oracle.step(p, None, (-1e9,) * 3, (1e9,) * 3, 0, x, np.zeros_like(x), f64=True)
+    x0 = np.asarray(x, np.float64)[rr["perm"][:rr["num"]]]
+    rho = np.zeros(len(x0))
+    for k in range(rr["nbr"].shape[1]):
+        sel = rr["nnb"] > k
+        q = rr["nbr"][sel, k]
+        d2 = ((x0[sel] - x0[q]) ** 2).sum(axis=1)
+        rho[sel] += m * 1.56668147065 / h ** 3 * np.clip(1 - d2 / h ** 2, 0, None) ** 3
+    return float(np.abs(rho / p["stable_density"] - 1).mean())
+
+
+# (lattice, box, scene id, steps): dam breaks with stable parameters, run up
+# to where FP32 rounding alone keeps both statistics within a few 0.1% of
+# FP64 (measured with the FP32 oracle: the 24^3 block within 1.5e-3 through
+# step 70, then the splash makes the flow chaotic, 1.5e-2 at step 80; the
+# 16^3 block within 5e-3 through step 50, 1.1e-2 at step 60)
+LONG_RUNS = [((24, 24, 24), (2.5, 2.0, 2.0), 79, 60), ((16, 16, 16), (2.0, 1.5, 1.5), 77, 40)]
+
+
+@pytest.mark.parametrize("lat,box,sid,steps", LONG_RUNS, ids=["24cubed_60", "16cubed_40"])
+def test_long_run_statistics_match_fp64_oracle(oracle, gpu, lat, box, sid, steps):
+    """Longer runs, checked statistically: every 20 steps the GPU run's mean
+    density error and kinetic energy are within 1% of the FP64 oracle run
+    from the same start (64 neighbour slots, s_corr k = 1e-4, the other
+    configured physics unchanged)."""
+    sc = scenes.dam_break(*lat, box, scene_id=sid)
     params = api.config_params(scorr_k=1e-4, max_pair_particle_num=64)
     p = H.resolved(params, sc)
     part = api.PbfParticle(p, sc.n, sc.domain_end)
     part.set_particles(sc.x, sc.v)
     b = H.gpu_boundary(sc, "planes")
     xo, vo = sc.x, sc.v
-    x32, v32 = sc.x, sc.v
-    for _ in range(60):
+    for s in range(1, steps + 1):
         api.one_step(part, b, sc.area, 4)
         r = H.run_oracle(oracle, sc, params, "planes", 4, f64=True, x=xo, v=vo)
         xo, vo = r["x"], r["v"]
-        r = H.run_oracle(oracle, sc, params, "planes", 4, f64=False, x=x32, v=v32)
-        x32, v32 = r["x"], r["v"]
-    xg, vg = part.get_particles()
-    m = p["particle_mass"]
-
-    def kinetic(v):
-        return 0.5 * m * float((v.astype(np.float64) ** 2).sum())
-
-    def mean_density_error(x):
-        # density from the oracle's neighbour lists of this configuration (one more step, 0 iterations)
-        rr = oracle.step(p, None, (-1e9,) * 3, (1e9,) * 3, 0, x, np.zeros_like(x), f64=True)
-        x0 = np.asarray(x, np.float64)[rr["perm"][:rr["num"]]]
-        h = p["smoothing_length"]
-        rho = np.zeros(len(x0))
-        for k in range(rr["nbr"].shape[1]):
-            sel = rr["nnb"] > k
-            q = rr["nbr"][sel, k]
-            d2 = ((x0[sel] - x0[q]) ** 2).sum(axis=1)
-            rho[sel] += m * 1.56668147065 / h ** 3 * np.clip(1 - d2 / h ** 2, 0, None) ** 3
-        return float(np.abs(rho / p["stable_density"] - 1).mean())
-
-    ke_g, ke_o, ke_32 = kinetic(vg), kinetic(vo), kinetic(v32)
-    assert abs(ke_g - ke_o) <= max(0.01 * ke_o, 2.0 * abs(ke_32 - ke_o))
-    de_g, de_o, de_32 = mean_density_error(xg), mean_density_error(xo), mean_density_error(x32)
-    assert abs(de_g - de_o) <= max(0.01 * de_o + 1e-4, 2.0 * abs(de_32 - de_o))
+        if s % 20 == 0:
+            xg, vg = part.get_particles()
+            assert len(xg) == len(xo)
+            ke_g, ke_o = _kinetic(p, vg), _kinetic(p, vo)
+            de_g, de_o = _mean_density_error(oracle, p, xg), _mean_density_error(oracle, p, xo)
+            print(f"{lat} step {s}: kinetic energy {ke_g:.6g} vs {ke_o:.6g} ({abs(ke_g - ke_o) / ke_o:.2e}), "
+                  f"mean density error {de_g:.6g} vs {de_o:.6g} ({abs(de_g - de_o) / de_o:.2e})")
+            assert abs(ke_g - ke_o) <= 0.01 * ke_o
+            assert abs(de_g - de_o) <= 0.01 * de_o
 
 
 @pytest.mark.parametrize("grid", [(4, 4, 4), (16, 8, 8), (16, 16, 8), (16, 16, 16), (32, 16, 16),
