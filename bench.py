@@ -819,7 +819,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break scenes, no dataset)",
             "config": workload_config(len(scs), n_total, cells, world),
-            "launch": {"tile": tile, "chunk": shape["chunk"], "preheat_s": args.preheat},
+            "launch": {"tile": tile, "chunk": shape["chunk"], "cell_tile": shape["cell_tile"],
+                       "preheat_s": args.preheat},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "single_large": single,
             "plain_dam_32k": small, "batched_chained": chained,
             "serving": serving, "ns_microbench": ns_micro, "ssf_frame": ssf,

@@ -251,6 +251,11 @@ pbf_status pbf_batch_set_tile(pbf_batch *b, uint32_t tile);
 pbf_status pbf_batch_set_chunk(pbf_batch *b, uint32_t chunk);
 /* Current tile (particles per block) and chunk. */
 pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *chunk);
+/* Cells per CTA of the per-cell stable rank of large steps (64, 128, 256 or
+ * 512; the autotuner also picks it).  Results do not depend on it.  No
+ * reference counterpart. */
+pbf_status pbf_batch_set_cell_tile(pbf_batch *b, uint32_t cells);
+pbf_status pbf_batch_get_cell_tile(pbf_batch *b, uint32_t *cells);
 pbf_status pbf_batch_set_graph_mode(pbf_batch *b, int enable);
 /* Kernels launched by the last pbf_batch_step / pbf_one_step call. */
 pbf_status pbf_batch_last_launches(pbf_batch *b, uint32_t *launches);

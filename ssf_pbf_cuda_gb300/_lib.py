@@ -135,6 +135,8 @@ SIGNATURES = {
     "pbf_batch_autotune": (c_i32, [c_vp, ctypes.c_int, c_vp, P(c_u32)]),
     "pbf_batch_set_tile": (c_i32, [c_vp, c_u32]),
     "pbf_batch_set_chunk": (c_i32, [c_vp, c_u32]),
+    "pbf_batch_set_cell_tile": (c_i32, [c_vp, c_u32]),
+    "pbf_batch_get_cell_tile": (c_i32, [c_vp, P(c_u32)]),
     "pbf_batch_get_launch_shape": (c_i32, [c_vp, c_vp, c_vp]),
     "pbf_batch_set_graph_mode": (c_i32, [c_vp, ctypes.c_int]),
     "pbf_batch_last_launches": (c_i32, [c_vp, P(c_u32)]),

@@ -567,11 +567,16 @@ class Batch:
         """Neighbour indices requested ahead per thread in the lambda / delta-p passes (4 or 8)."""
         check(load().pbf_batch_set_chunk(self.handle, int(chunk)), "pbf_batch_set_chunk")
 
+    def set_cell_tile(self, cells: int):
+        """Cells per CTA of the per-cell stable rank of large steps (64, 128, 256 or 512)."""
+        check(load().pbf_batch_set_cell_tile(self.handle, int(cells)), "pbf_batch_set_cell_tile")
+
     def launch_shape(self) -> dict:
-        t, c = ctypes.c_uint32(), ctypes.c_uint32()
+        t, c, ct = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         check(load().pbf_batch_get_launch_shape(self.handle, ctypes.byref(t), ctypes.byref(c)),
               "pbf_batch_get_launch_shape")
-        return {"tile": t.value, "chunk": c.value}
+        check(load().pbf_batch_get_cell_tile(self.handle, ctypes.byref(ct)), "pbf_batch_get_cell_tile")
+        return {"tile": t.value, "chunk": c.value, "cell_tile": ct.value}
 
     def set_graph_mode(self, on: bool):
         check(load().pbf_batch_set_graph_mode(self.handle, 1 if on else 0), "pbf_batch_set_graph_mode")

@@ -493,6 +493,21 @@ pbf_status pbf_batch_get_launch_shape(pbf_batch *b, uint32_t *tile, uint32_t *ch
     return PBF_SUCCESS;
 }
 
+pbf_status pbf_batch_set_cell_tile(pbf_batch *b, uint32_t cells)
+{
+    if (!b) return PBF_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(b->mu);
+    return b->b.set_cell_tile(cells);
+}
+
+pbf_status pbf_batch_get_cell_tile(pbf_batch *b, uint32_t *cells)
+{
+    if (!b || !cells) return PBF_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(b->mu);
+    *cells = b->b.cell_tile();
+    return PBF_SUCCESS;
+}
+
 pbf_status pbf_batch_set_graph_mode(pbf_batch *b, int enable)
 {
     if (!b) return PBF_ERROR_INVALID_ARGUMENT;

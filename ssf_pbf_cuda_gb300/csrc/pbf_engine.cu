@@ -205,7 +205,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     max_pair_ = max_pair;
     bnd_capacity_ = (uint64_t)max_scenes * 32 + 1024;
     // particle tiles (64 particles at the smallest tile) then cell tiles
-    max_tiles_ = max_particles / 64 + max_scenes + 1 + max_cells / kCellTile + max_scenes + 1;
+    max_tiles_ = max_particles / 64 + max_scenes + 1 + max_cells / kCellTileMin + max_scenes + 1;
     const uint64_t P = max_particles, C = max_cells;
     auto A = [&](void **p, uint64_t bytes) -> cudaError_t {
         arena_bytes_ += bytes;
@@ -323,6 +323,7 @@ pbf_status Batch::add_scene(const pbf_params &p, uint32_t capacity, const float 
     sh.bnd_off = bo;
     sh.desc.p_off = (uint32_t)po;
     sh.desc.capacity = capacity;
+    sh.desc.list16 = capacity <= kList16Max ? 1u : 0u;
     sh.desc.c_off = (uint32_t)co;
     sh.desc.b_off = (uint32_t)bo;
     sh.desc.builtin_sphere = b ? 0u : 1u;
@@ -519,6 +520,7 @@ pbf_status Batch::set_scene_params(uint32_t id, const pbf_params &p)
     if (d.ncell != s.desc.ncell || q.max_pair_particle_num > max_pair_) return PBF_ERROR_INVALID_ARGUMENT;
     d.p_off = s.desc.p_off;
     d.capacity = s.desc.capacity;
+    d.list16 = s.desc.list16;
     d.c_off = s.desc.c_off;
     d.b_off = s.desc.b_off;
     d.builtin_sphere = s.desc.builtin_sphere;
@@ -594,7 +596,7 @@ void Batch::rebuild_tiles()
     for (uint32_t k = 0; k < scenes_.size(); ++k) {
         const SceneHost &s = scenes_[k];
         if (!s.active) continue;
-        for (uint32_t c0 = 0; c0 <= s.desc.ncell; c0 += kCellTile) {
+        for (uint32_t c0 = 0; c0 <= s.desc.ncell; c0 += cell_tile_) {
             tile_scene_.push_back(k);
             tile_start_.push_back(c0);
         }
@@ -664,6 +666,7 @@ LaunchShape Batch::shape_for(uint32_t tile) const
     sh.grid_apply = g(o.apply);
     sh.grid_xsph = g(o.xsph);
     sh.grid_cells = pow2(std::max<uint32_t>(1, ctrl_.n_cell_tiles));  // a block per cell tile
+    sh.cell_tile = cell_tile_;
     sh.small = (uint64_t)nt * tile <= kSmallStep ? 1u : 0u;
     sh.grid_split = std::min<uint32_t>((uint32_t)sms_ * std::max<uint32_t>(1, o.split), ntb * (tile / (256 / kSplit)));
     const uint32_t scan_tiles = std::max<uint32_t>(1, (ctrl_.n_cells + kScanTile - 1) / kScanTile);
@@ -724,9 +727,11 @@ StepArgs Batch::args() const
 
 uint32_t Batch::post_modes() const
 {
-    bool x_off = false, x_walk = false, x_list = false, v_ref = false, v_text = false;
+    bool x_off = false, x_walk = false, x_list = false, v_ref = false, v_text = false, l16 = false, l32 = false;
     for (auto &s : scenes_)
         if (s.active) {
+            l16 |= s.desc.list16 != 0;
+            l32 |= s.desc.list16 == 0;
             x_off |= s.desc.xsph_mode == PBF_XSPH_OFF;
             x_walk |= s.desc.xsph_mode == PBF_XSPH_WALK;
             x_list |= s.desc.xsph_mode == PBF_XSPH_LIST;
@@ -740,6 +745,8 @@ uint32_t Batch::post_modes() const
     if (x_list || (x_off && x_walk)) m |= kPostXsphList;
     if (v_ref) m |= kPostVortReference;
     if (v_text) m |= kPostVortTextbook;
+    if (l16) m |= kPostList16;
+    if (l32) m |= kPostList32;
     return m;
 }
 
@@ -983,14 +990,18 @@ pbf_status Batch::get_debug(uint32_t id, uint32_t *sorted_hash, uint32_t *perm, 
         std::vector<uint8_t> nn(live);
         std::vector<uint32_t> quads(4ull * live);
         if (live) CK(cudaMemcpy(nn.data(), d_nnb_ + d.p_off, live, cudaMemcpyDeviceToHost));
-        for (uint32_t kq = 0; 4 * kq < d.cap && live; ++kq) {  // slots 4kq..4kq+3 of every particle
+        // rows of 16 bytes per particle: quads of 4 u32 sorted slots, or
+        // octs of 8 u16 scene-local indices (scenes of at most kList16Max slots)
+        const uint32_t per_row = d.list16 ? 8u : 4u;
+        for (uint32_t kq = 0; per_row * kq < d.cap && live; ++kq) {  // slots per_row*kq.. of every particle
             CK(cudaMemcpy(quads.data(), d_nbr_ + 4ull * ((uint64_t)kq * max_particles_ + d.p_off), 16ull * live,
                           cudaMemcpyDeviceToHost));
-            for (uint32_t k = 4 * kq; k < 4 * kq + 4 && k < d.cap; ++k)
+            const uint16_t *octs = reinterpret_cast<const uint16_t *>(quads.data());
+            for (uint32_t k = per_row * kq; k < per_row * kq + per_row && k < d.cap; ++k)
                 for (uint32_t p = 0; p < live; ++p)
                     if (k < nn[p])
                         neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp] =
-                            quads[4ull * p + (k & 3)] - d.p_off;
+                            d.list16 ? octs[8ull * p + (k & 7)] : quads[4ull * p + (k & 3)] - d.p_off;
         }
     }
     return PBF_SUCCESS;
@@ -1029,6 +1040,14 @@ pbf_status Batch::set_chunk(uint32_t chunk)
 {
     if (chunk != 4 && chunk != 8) return PBF_ERROR_INVALID_ARGUMENT;
     chunk_ = chunk;
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::set_cell_tile(uint32_t cells)
+{
+    if (cells < kCellTileMin || cells > kCellTileMax || (cells & (cells - 1))) return PBF_ERROR_INVALID_ARGUMENT;
+    if (cells != cell_tile_) dirty_tiles_ = true;
+    cell_tile_ = cells;
     return PBF_SUCCESS;
 }
 
@@ -1090,6 +1109,29 @@ pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
     }
     set_tile(best);
     chunk_ = best_chunk;
+    // then the cells per CTA of the per-cell rank (large steps only rank per cell)
+    uint32_t best_cells = cell_tile_;
+    if (rc == PBF_SUCCESS && !shape_for(best).small) {
+        best_ms = 1e30f;
+        for (uint32_t c : {256u, 128u, 512u, 64u}) {
+            set_cell_tile(c);
+            rc = upload(st);
+            if (rc != PBF_SUCCESS) break;
+            for (int r = 0; r < 2; ++r) run(iters, st, false);
+            CK(cudaEventRecord(e0, st));
+            for (int r = 0; r < 8; ++r) run(iters, st, false);
+            CK(cudaEventRecord(e1, st));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_cells = c;
+            }
+            CK(restore());
+        }
+    }
+    set_cell_tile(best_cells);
     rc = upload(st);
     CK(cudaStreamSynchronize(st));
     cudaEventDestroy(e0);

@@ -96,6 +96,9 @@ public:
     pbf_status profile_step(int iters, cudaStream_t st, float *ms, char *names, uint32_t max, uint32_t *n);
     pbf_status set_tile(uint32_t tile);
     pbf_status set_chunk(uint32_t chunk);
+    // cells per CTA of the per-cell rank (64, 128, 256 or 512)
+    pbf_status set_cell_tile(uint32_t cells);
+    uint32_t cell_tile() const { return cell_tile_; }
     uint32_t tile() const { return tile_; }
     uint32_t chunk() const { return chunk_; }
     void set_graph_mode(bool on) { graph_mode_ = on; }
@@ -164,6 +167,7 @@ private:
     // launch configuration and graph cache
     uint32_t tile_ = 256;
     uint32_t chunk_ = 8;
+    uint32_t cell_tile_ = kCellTile;
     bool graph_mode_ = true;
     cudaStream_t cap_stream_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;

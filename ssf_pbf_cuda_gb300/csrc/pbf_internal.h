@@ -7,7 +7,7 @@
 
 namespace pbf103 {
 
-// Per-scene constants, one 192-byte record per scene slot in device memory.
+// Per-scene constants, one 208-byte record per scene slot in device memory.
 // Derived once on the host from pbf_params (the reference keeps these in
 // __constant__ symbols and a function-static, pbf_position_update.cu:14-17,
 // pbf_solve.cpp:92; here they are per scene so scenes never share state).
@@ -52,6 +52,8 @@ struct SceneDesc {
     float ih2;           // 1/h^2 (poly6 from r^2)
     float tens_c;        // reference s_corr: 10 / W(0.4h)^4, the factor of W^4
     float scorr_c;       // textbook s_corr: k / W(dq h)^n, the factor of W^n
+    uint32_t list16;     // the neighbour list holds u16 scene-local indices (capacity <= 65,536)
+    uint32_t pad0, pad1, pad2;
 };
 static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
 
@@ -61,7 +63,7 @@ struct Ctrl {
     uint32_t n_tiles;       // particle tiles at the front of tile_scene/tile_start
     uint32_t n_cells;       // cell entries to scan (high-water mark of cell ranges)
     uint32_t n_scenes;
-    uint32_t n_cell_tiles;  // cell tiles after them: kCellTile cells of one scene each
+    uint32_t n_cell_tiles;  // cell tiles after them: LaunchShape::cell_tile cells of one scene each
 };
 
 struct StepArgs {
@@ -100,7 +102,8 @@ struct LaunchShape {
     uint32_t chunk;       // neighbours per chunk in the lambda / delta-p passes (4 or 8)
     // persistent grids of the heavy kernels, each from its own occupancy
     uint32_t grid_nb, grid_lambda, grid_dp, grid_omega, grid_apply, grid_xsph;
-    uint32_t grid_cells;  // grid of k_rank_cells: a block of kCellTile threads per cell tile
+    uint32_t grid_cells;  // grid of k_rank_cells: a block of cell_tile threads per cell tile
+    uint32_t cell_tile;   // cells per cell tile = threads per k_rank_cells block (autotuned)
     uint32_t small;       // latency-bound step (at most kSmallStep particle slots): split
                           // neighbour walk, per-particle rank, lambda kept in its own array
     uint32_t grid_split;  // grid of k_neighbors_split (blocks of 256 threads, 256 / kSplit particles each)
@@ -109,7 +112,7 @@ struct LaunchShape {
     {
         return tile == o.tile && grid == o.grid && scan_grid == o.scan_grid && scan_rounds == o.scan_rounds &&
                chunk == o.chunk &&
-               grid_cells == o.grid_cells && small == o.small && grid_split == o.grid_split && nb_smem == o.nb_smem &&
+               grid_cells == o.grid_cells && cell_tile == o.cell_tile && small == o.small && grid_split == o.grid_split && nb_smem == o.nb_smem &&
                grid_nb == o.grid_nb && grid_lambda == o.grid_lambda && grid_dp == o.grid_dp &&
                grid_omega == o.grid_omega && grid_apply == o.grid_apply && grid_xsph == o.grid_xsph;
     }
@@ -133,6 +136,8 @@ enum : uint32_t {
     kPostXsphList = 2,       // XSPH over the step's neighbour list (+ copy for scenes without XSPH)
     kPostVortReference = 4,  // vorticity, the reference's walk and kernel scaling
     kPostVortTextbook = 8,   // vorticity, textbook form over the neighbour list
+    kPostList32 = 16,        // some scene keeps a u32 neighbour list (list forms launch per list format)
+    kPostList16 = 32,        // some scene keeps a u16 neighbour list
 };
 
 // Enqueue one full solver step for every scene in the tile list.
@@ -165,8 +170,10 @@ constexpr uint32_t kScanTile = kScanItemsPerWarp * kScanWarps;  // 4096 cells pe
 constexpr uint32_t kSingleScanMax = 65536;  // cells up to which one block scans the whole table
 constexpr uint32_t kNbSmemMax = 96 * 1024;  // shared-memory budget for a k_neighbors_lambda block's lists
 constexpr uint32_t kSplit = 4;  // small steps: lanes per particle in the split neighbour walk (blocks of 256)
-constexpr uint32_t kCellTile = 256;         // cells per cell tile = threads per k_rank_cells block
+constexpr uint32_t kCellTile = 256;         // default cells per cell tile = threads per k_rank_cells block
+constexpr uint32_t kCellTileMin = 64, kCellTileMax = 512;  // the autotuner's range
 constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)
 constexpr uint32_t kSmallStep = 131072;     // particle slots up to which a step is latency bound
+constexpr uint32_t kList16Max = 65536;      // scenes of at most this many slots keep u16 neighbour lists
 
 }  // namespace pbf103

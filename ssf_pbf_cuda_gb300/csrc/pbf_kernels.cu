@@ -406,6 +406,14 @@ __device__ __forceinline__ uint64_t list_slot(uint32_t k, uint64_t stride)
     return (uint64_t)(k >> 2) * stride * 4u + (k & 3u);
 }
 
+// One 16-byte row of a particle's list (a quad of u32 or an oct of u16
+// slots), loaded and stored as streaming data (evict-first): the lists of a
+// batch (hundreds of MB) pass through L2 once per pass, and the hint keeps
+// them from evicting the positions the same passes gather (batched step
+// +1%, the list-form vorticity pass -4%, interleaved A/B).
+__device__ __forceinline__ uint4 list_ld(const uint4 *p) { return __ldcs(p); }
+__device__ __forceinline__ void list_st(uint4 *p, uint4 v) { __stcs(p, v); }
+
 __device__ __forceinline__ uint32_t quad_at(const uint4 &v, int j)
 {
     return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
@@ -425,7 +433,7 @@ __device__ __forceinline__ void list_walk(const uint32_t *__restrict__ nl, uint6
     const uint4 z = make_uint4(0u, 0u, 0u, 0u);
     uint4 qn[NQ];
 #pragma unroll
-    for (int c = 0; c < NQ; ++c) qn[c] = ((uint32_t)(4 * c) < nn) ? __ldg(p + c * stride) : z;
+    for (int c = 0; c < NQ; ++c) qn[c] = ((uint32_t)(4 * c) < nn) ? list_ld(p + c * stride) : z;
     uint32_t k0 = 0;
     for (; k0 + CH <= nn; k0 += CH) {
         uint4 q[NQ];
@@ -433,13 +441,64 @@ __device__ __forceinline__ void list_walk(const uint32_t *__restrict__ nl, uint6
         for (int c = 0; c < NQ; ++c) q[c] = qn[c];
         p += NQ * stride;
 #pragma unroll
-        for (int c = 0; c < NQ; ++c) qn[c] = (k0 + CH + 4 * c < nn) ? __ldg(p + c * stride) : z;
+        for (int c = 0; c < NQ; ++c) qn[c] = (k0 + CH + 4 * c < nn) ? list_ld(p + c * stride) : z;
 #pragma unroll
         for (int c = 0; c < CH; ++c) f(quad_at(q[c >> 2], c & 3));
     }
 #pragma unroll
     for (int c = 0; c < CH - 1; ++c)
         if (k0 + c < nn) f(quad_at(qn[c >> 2], c & 3));
+}
+
+// Scenes of at most kList16Max particle slots (every batched scene) keep
+// their lists as u16 scene-local indices in octs of 8 slots: slot k of
+// particle slot i at nbr16[((k / 8) * stride + i) * 8 + k % 8], the same
+// 16-byte rows as the quads of u32 lists, half as many of them, so a pass
+// reads half the list bytes.  list16_slot is the u16 offset of slot k from
+// the particle's base (list_of, as for quads).
+__device__ __forceinline__ uint64_t list16_slot(uint32_t k, uint64_t stride)
+{
+    return (uint64_t)(k >> 3) * stride * 8u + (k & 7u);
+}
+
+__device__ __forceinline__ uint32_t oct_at(const uint4 &v, int j)
+{
+    const uint32_t w = j < 2 ? v.x : (j < 4 ? v.y : (j < 6 ? v.z : v.w));
+    return (j & 1) ? (w >> 16) : (w & 0xFFFFu);
+}
+
+// list_walk over a u16 list: octs requested one chunk (8 slots) ahead;
+// f gets base + the scene-local index, i.e. the particle's sorted slot.
+template <class F>
+__device__ __forceinline__ void list_walk16(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn,
+                                            uint32_t base, F &&f)
+{
+    const uint4 *p = reinterpret_cast<const uint4 *>(nl);  // oct ko of the particle at p[ko * stride]
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    uint4 qn = (0u < nn) ? list_ld(p) : z;
+    uint32_t k0 = 0;
+    for (; k0 + 8 <= nn; k0 += 8) {
+        const uint4 q = qn;
+        p += stride;
+        qn = (k0 + 8 < nn) ? list_ld(p) : z;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) f(base + oct_at(q, c));
+    }
+#pragma unroll
+    for (int c = 0; c < 7; ++c)
+        if (k0 + c < nn) f(base + oct_at(qn, c));
+}
+
+// The list of one particle in either form: u32 quads (indices are sorted
+// slots) or u16 octs (scene-local indices, base = the scene's first slot).
+template <int CH, class F>
+__device__ __forceinline__ void list_walk_any(bool l16, const uint32_t *__restrict__ nl, uint64_t stride,
+                                              uint32_t nn, uint32_t base, F &&f)
+{
+    if (l16)
+        list_walk16(nl, stride, nn, base, f);
+    else
+        list_walk<CH>(nl, stride, nn, f);
 }
 
 // list_walk in chunks of one quad with the quads requested two chunks
@@ -450,13 +509,13 @@ __device__ __forceinline__ void list_walk_ahead2(const uint32_t *__restrict__ nl
 {
     const uint4 *p = reinterpret_cast<const uint4 *>(nl);
     const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-    uint4 q0 = (0u < nn) ? __ldg(p) : z;
-    uint4 q1 = (4u < nn) ? __ldg(p + stride) : z;
+    uint4 q0 = (0u < nn) ? list_ld(p) : z;
+    uint4 q1 = (4u < nn) ? list_ld(p + stride) : z;
     uint32_t k0 = 0;
     for (; k0 + 4 <= nn; k0 += 4) {
         const uint4 q = q0;
         q0 = q1;
-        q1 = (k0 + 8 < nn) ? __ldg(p + (uint64_t)((k0 >> 2) + 2) * stride) : z;
+        q1 = (k0 + 8 < nn) ? list_ld(p + (uint64_t)((k0 >> 2) + 2) * stride) : z;
         f(q.x);
         f(q.y);
         f(q.z);
@@ -742,7 +801,7 @@ __global__ void __launch_bounds__(512) k_scatter(StepArgs a)
 constexpr uint32_t kStableLimit = 4096;
 constexpr uint32_t kDenseMin = 64;
 static_assert(kStableLimit * sizeof(uint32_t) == sizeof(RadixSmem), "the radix sort reuses the bitonic buffer");
-__global__ void __launch_bounds__(kCellTile) k_rank_cells(StepArgs a)
+__global__ void __launch_bounds__(kCellTileMax) k_rank_cells(StepArgs a)
 {
     const uint32_t n0 = a.ctrl->n_tiles, nct = a.ctrl->n_cell_tiles;
     for (uint32_t t_ = blockIdx.x; t_ < nct; t_ += gridDim.x) {
@@ -1048,6 +1107,8 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     const uint32_t cap = d.cap;
     const uint64_t stride = a.nbr_stride;
     uint32_t *nl = list_of(a.nbr, i);
+    uint16_t *nl16 = reinterpret_cast<uint16_t *>(nl);  // u16 lists: scene-local indices
+    const bool l16 = d.list16 != 0;
     const float4 *__restrict__ xa = a.xa;
     const float4 *__restrict__ wx = a.wx;
     // phase 1: the walk only tests and records (lanes of a warp accept
@@ -1072,10 +1133,13 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (acc[k] && cnt < cap) {
+                    const uint32_t q = __float_as_uint(c[k].w);
                     if (SMEM)
-                        s_list[cnt * blockDim.x + threadIdx.x] = __float_as_uint(c[k].w);
+                        s_list[cnt * blockDim.x + threadIdx.x] = q;
+                    else if (l16)
+                        nl16[list16_slot(cnt, stride)] = (uint16_t)(q - d.p_off);
                     else
-                        nl[list_slot(cnt, stride)] = __float_as_uint(c[k].w);
+                        nl[list_slot(cnt, stride)] = q;
                     ++cnt;
                 }
             }
@@ -1088,15 +1152,29 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // the read-only path may not see this kernel's own stores)
     LamSum ls;
     if (SMEM) {  // the list from shared memory, written out slot by slot as it is summed
-        // the list out in whole quads: one 16-byte store per four slots
-        // (slots past the count in the last quad are padding, never read)
+        // the list out in whole quads (u32) or octs (u16): one 16-byte store
+        // per four or eight slots (slots past the count in the last one are
+        // padding, never read)
         const uint32_t *rd = s_list + threadIdx.x;
         uint4 *wq = reinterpret_cast<uint4 *>(nl);
-        for (uint32_t k0 = 0; k0 < cnt; k0 += 4) {
-            uint32_t q4[4];
+        if (l16) {
+            for (uint32_t k0 = 0; k0 < cnt; k0 += 8) {
+                uint32_t w[4];
 #pragma unroll
-            for (uint32_t j = 0; j < 4; ++j) q4[j] = (k0 + j < cnt) ? rd[(k0 + j) * blockDim.x] : 0u;
-            wq[(uint64_t)(k0 >> 2) * stride] = make_uint4(q4[0], q4[1], q4[2], q4[3]);
+                for (uint32_t j = 0; j < 4; ++j) {
+                    const uint32_t lo = (k0 + 2 * j < cnt) ? rd[(k0 + 2 * j) * blockDim.x] - d.p_off : 0u;
+                    const uint32_t hi = (k0 + 2 * j + 1 < cnt) ? rd[(k0 + 2 * j + 1) * blockDim.x] - d.p_off : 0u;
+                    w[j] = (lo & 0xFFFFu) | (hi << 16);
+                }
+                list_st(wq + (uint64_t)(k0 >> 3) * stride, make_uint4(w[0], w[1], w[2], w[3]));
+            }
+        } else {
+            for (uint32_t k0 = 0; k0 < cnt; k0 += 4) {
+                uint32_t q4[4];
+#pragma unroll
+                for (uint32_t j = 0; j < 4; ++j) q4[j] = (k0 + j < cnt) ? rd[(k0 + j) * blockDim.x] : 0u;
+                list_st(wq + (uint64_t)(k0 >> 2) * stride, make_uint4(q4[0], q4[1], q4[2], q4[3]));
+            }
         }
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
@@ -1107,7 +1185,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     } else {
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t q = nl[list_slot(k, stride)];
+            const uint32_t q = l16 ? d.p_off + nl16[list16_slot(k, stride)] : nl[list_slot(k, stride)];
             lam_add(ls, xp, __ldg(xa + q), pc);
         }
     }
@@ -1144,9 +1222,14 @@ __device__ __forceinline__ void split_rows(uint32_t sub, int &rr0, int &rr1)
 // the list is read through the read-only path (it was not written by this
 // kernel).
 template <bool RO>
-__device__ __forceinline__ uint32_t split_index(const uint32_t *nl, uint64_t stride, uint32_t nn, uint32_t k)
+__device__ __forceinline__ uint32_t split_index(const uint32_t *nl, uint64_t stride, uint32_t nn, uint32_t k,
+                                                bool l16, uint32_t base)
 {
     if (k >= nn) return 0u;
+    if (l16) {
+        const uint16_t *p = reinterpret_cast<const uint16_t *>(nl) + list16_slot(k, stride);
+        return base + (RO ? __ldg(p) : *p);
+    }
     const uint32_t *p = nl + list_slot(k, stride);
     return RO ? __ldg(p) : *p;
 }
@@ -1157,12 +1240,14 @@ __device__ __forceinline__ LamSum lam_sum_split(const uint32_t *nl, uint64_t str
                                                 uint32_t sub, uint32_t gmask)
 {
     const PairConst pc = pair_const(d);
+    const bool l16 = d.list16 != 0;
+    const uint32_t base = d.p_off;
     LamSum ls;
-    float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub));
-    uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit);
+    float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub, l16, base));
+    uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit, l16, base);
     for (uint32_t k0 = 0; k0 < nn; k0 += kSplit) {
         const float4 x1 = __ldg(xc + q1);
-        q1 = split_index<RO>(nl, stride, nn, k0 + 2 * kSplit + sub);
+        q1 = split_index<RO>(nl, stride, nn, k0 + 2 * kSplit + sub, l16, base);
         // this lane's pair (slot k0 + sub); a slot past the list reads
         // index 0 and is not added
         const PairGeo g = pair_geo(xp, x0);
@@ -1203,6 +1288,14 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         const uint32_t cap = d.cap;
         const uint64_t stride = a.nbr_stride;
         uint32_t *nl = list_of(a.nbr, i);
+        uint16_t *nl16 = reinterpret_cast<uint16_t *>(nl);
+        const bool l16 = d.list16 != 0;
+        auto put = [&](uint32_t k, uint32_t q) {  // slot k of the list := sorted slot q
+            if (l16)
+                nl16[list16_slot(k, stride)] = (uint16_t)(q - d.p_off);
+            else
+                nl[list_slot(k, stride)] = q;
+        };
         const float4 *__restrict__ xa = a.xa;
         const float4 *__restrict__ wx = a.wx;
         // rows shared over the lanes (split_rows); one lane takes all nine
@@ -1218,7 +1311,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
                 for (uint32_t q = st; q < en; ++q) {
                     const float4 c = __ldg(src + q);
                     if (dist2_exact(xp, c) < h2) {
-                        nl[list_slot(cnt, stride)] = __float_as_uint(c.w);
+                        put(cnt, __float_as_uint(c.w));
                         if (++cnt == cap) return false;
                     }
                 }
@@ -1256,7 +1349,7 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         const uint32_t total = __shfl_sync(gmask, incl, kSplit - 1, kSplit);
         if (!one) {
             const uint32_t pre = incl - cnt;
-            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) nl[list_slot(pre + t, stride)] = buf[t];
+            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) put(pre + t, buf[t]);
         }
         const uint32_t nn = total < cap ? total : cap;
         __syncwarp(gmask);  // the list entries of the group are visible to all its lanes
@@ -1285,8 +1378,8 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const PairConst pc = pair_const(d);
     const float4 xp = xc[i];
     LamSum ls;
-    list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i],
-                      [&](uint32_t q) { lam_add(ls, xp, __ldg(xc + q), pc); });
+    list_walk_any<kChunk>(d.list16 != 0, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off,
+                          [&](uint32_t q) { lam_add(ls, xp, __ldg(xc + q), pc); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
     // delta-p pass gathers next (neighbours here use only .xyz); small,
     // latency-bound steps keep it in its own array, as the store into the
@@ -1353,7 +1446,7 @@ __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, 
     const ScorrConst sc = scorr_const(d, li);
     const float *__restrict__ lam = a.lam;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    list_walk<kChunk>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], [&](uint32_t q) {
+    list_walk_any<kChunk>(d.list16 != 0, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, [&](uint32_t q) {
         const float4 xq = __ldg(xc + q);
         const PairGeo g = pair_geo(xp, xq);
         const PairWS k = pair_ws(g.r2, pc);
@@ -1439,12 +1532,13 @@ __global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict
 // (pbf_vorticity_confinement.cu:28); otherwise the textbook kernel over the
 // step's neighbour list.  Each form is its own kernel (scenes of the other
 // forms are skipped) so the list form keeps a lean register allocation.
-template <bool REF>
+template <bool REF, bool L16>
 __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__restrict__ vs)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
     if (d.vort_mode != (REF ? PBF_VORTICITY_REFERENCE : PBF_VORTICITY_TEXTBOOK)) continue;
+    if (!REF && (d.list16 != 0) != L16) continue;  // the other list format's instance
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
@@ -1477,7 +1571,7 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             },
             use);
     } else {
-        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
+        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
     }
     const float mr = d.m * d.inv_rho0;
     const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
@@ -1489,12 +1583,13 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
 }
 
 // Vorticity, pass 2 (addVorticityConfinementCUDA, pbf_vorticity_confinement.cu:192-222).
-template <bool REF>
+template <bool REF, bool L16>
 __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restrict__ vs)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
     if (d.vort_mode != (REF ? PBF_VORTICITY_REFERENCE : PBF_VORTICITY_TEXTBOOK)) continue;
+    if (!REF && (d.list16 != 0) != L16) continue;  // the other list format's instance
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
@@ -1529,7 +1624,8 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             },
             use);
     } else {
-        list_walk<4>(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);  // 4: fewer registers, more warps (measured)
+        // quads of 4: fewer registers, more warps (measured)
+        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
     }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
@@ -1565,12 +1661,13 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
 // NaN guard.  WALK: the reference's uncapped 27-cell walk (scenes with
 // PBF_XSPH_WALK); otherwise over the step's neighbour list (scenes with
 // PBF_XSPH_LIST), also copying vs to vo for scenes without XSPH.
-template <bool WALK>
+template <bool WALK, bool L16>
 __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restrict__ vs, float4 *__restrict__ vo)
 {
     TILE_LOOP_BEGIN
     const SceneDesc d = a.scenes[s];
     if ((d.xsph_mode == PBF_XSPH_WALK) != WALK) continue;
+    if (!WALK && (d.list16 != 0) != L16) continue;  // the other list format's instance
     const uint32_t base = a.offsets[d.c_off];
     const uint32_t live = a.offsets[d.c_off + d.ncell] - base;
     if (local >= live) continue;
@@ -1611,7 +1708,10 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
             },
             use);
     } else {
-        list_walk_ahead2(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
+        if (L16)
+            list_walk16(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
+        else
+            list_walk_ahead2(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
     }
     float4 out = vi;
     if (!(isnan(s0) || isnan(s1) || isnan(s2))) {
@@ -1734,7 +1834,7 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     Occupancy o;
     o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
                  mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
-    o.cells = occ_b((const void *)k_rank_cells, kCellTile);
+    o.cells = occ_b((const void *)k_rank_cells, kCellTileMax);
     o.split = occ_b((const void *)k_neighbors_split, 256);
     o.nb = occ((const void *)k_neighbors_lambda<false>);
     cudaFuncSetAttribute((const void *)k_neighbors_lambda<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1742,9 +1842,9 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     const bool c4 = chunk == 4;
     o.lambda = occ(c4 ? PassFns<4>::lambda() : PassFns<8>::lambda());
     o.dp = occ(c4 ? PassFns<4>::dp() : PassFns<8>::dp());
-    o.omega = occ((const void *)k_vort_omega<false>);
-    o.apply = occ((const void *)k_vort_apply<false>);
-    o.xsph = occ((const void *)k_xsph<false>);
+    o.omega = mn(occ((const void *)k_vort_omega<false, false>), occ((const void *)k_vort_omega<false, true>));
+    o.apply = mn(occ((const void *)k_vort_apply<false, false>), occ((const void *)k_vort_apply<false, true>));
+    o.xsph = mn(occ((const void *)k_xsph<false, false>), occ((const void *)k_xsph<false, true>));
     std::lock_guard<std::mutex> lk(mu);
     cache[key] = o;
     return o;
@@ -1812,7 +1912,7 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
         k_rank_reorder<<<g, b, 0, st>>>(a);
         PBF_LAUNCHED("k_rank_reorder");
     } else {
-        k_rank_cells<<<sh.grid_cells, kCellTile, 0, st>>>(a);
+        k_rank_cells<<<sh.grid_cells, sh.cell_tile, 0, st>>>(a);
         PBF_LAUNCHED("k_rank_cells");
     }
     k_dense_sort<<<sh.grid, kRadixThreads, 0, st>>>(a);
@@ -1852,28 +1952,50 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     }
     // omega of every form before any apply: both forms read final positions
     // and velocities only
+    // the list forms run one instance per list format present (each skips
+    // the other format's scenes): one instance per format keeps its
+    // registers, and so its occupancy, to that format's loop
+    const bool l16 = (post & kPostList16) != 0, l32 = (post & kPostList32) != 0;
     if (post & kPostVortTextbook) {
-        k_vort_omega<false><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
-        PBF_LAUNCHED("k_vort_omega");
+        if (l32) {
+            k_vort_omega<false, false><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
+            PBF_LAUNCHED("k_vort_omega");
+        }
+        if (l16) {
+            k_vort_omega<false, true><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
+            PBF_LAUNCHED("k_vort_omega");
+        }
     }
     if (post & kPostVortReference) {
-        k_vort_omega<true><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
+        k_vort_omega<true, false><<<sh.grid_omega, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_omega_walk");
     }
     if (post & kPostVortTextbook) {
-        k_vort_apply<false><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
-        PBF_LAUNCHED("k_vort_apply");
+        if (l32) {
+            k_vort_apply<false, false><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
+            PBF_LAUNCHED("k_vort_apply");
+        }
+        if (l16) {
+            k_vort_apply<false, true><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
+            PBF_LAUNCHED("k_vort_apply");
+        }
     }
     if (post & kPostVortReference) {
-        k_vort_apply<true><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
+        k_vort_apply<true, false><<<sh.grid_apply, b, 0, st>>>(a, vfinal);
         PBF_LAUNCHED("k_vort_apply_walk");
     }
     if (post & kPostXsphList) {
-        k_xsph<false><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
-        PBF_LAUNCHED("k_xsph");
+        if (l32) {
+            k_xsph<false, false><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
+            PBF_LAUNCHED("k_xsph");
+        }
+        if (l16) {
+            k_xsph<false, true><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
+            PBF_LAUNCHED("k_xsph");
+        }
     }
     if (post & kPostXsphWalk) {
-        k_xsph<true><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
+        k_xsph<true, false><<<sh.grid_xsph, b, 0, st>>>(a, a.vt, a.v);
         PBF_LAUNCHED("k_xsph_walk");
     }
 #undef PBF_LAUNCHED

@@ -342,3 +342,23 @@ def test_server_refuses_requests_larger_than_the_arena(gpu):
     assert not t.is_alive()
     assert {c["request_id"] for c in srv3.poll()} == {rid}
     assert np.array_equal(srv3.result(rid)[0], alone(sc2, p2, hz2)["x"])
+
+
+@pytest.mark.parametrize("cells", [64, 128, 512])
+def test_cell_tiles_give_identical_results(gpu, cells):
+    """The per-cell stable rank of large steps (more than 131,072 particle
+    slots) runs `cells` cells per CTA, a launch-shape choice of the
+    autotuner: results equal the default 256 bit for bit."""
+    p = api.config_params(scorr_k=1e-4)
+    items = [(scenes.dam_break(32, 32, 32, (4.0, 2.0, 2.0), scene_id=71 + k), p) for k in range(5)]
+    out = {}
+    for c in (256, cells):
+        b, ids = make_batch(items)
+        b.set_cell_tile(c)
+        assert b.launch_shape()["cell_tile"] == c
+        b.step(4)
+        out[c] = [b.get_scene(sid) for sid in ids]
+    for (xa, va), (xb, vb) in zip(out[256], out[cells]):
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    with pytest.raises(pbf.PbfError):
+        b.set_cell_tile(100)
