@@ -284,6 +284,35 @@ static void fill_boundary(const pbf_boundary_t *b, std::vector<float4> &out)
     out = b->prims;
 }
 
+// The clear box of a boundary made only of planes whose normals are unit
+// axes (a box's walls).  For such a plane responsePlaneBoundary's
+// (p - on) . n is +-(p_c - on_c) exactly, so p hits none of them when
+// on_c <= p_c for each +e_c plane and p_c <= on_c for each -e_c plane:
+// box_lo / box_hi are the largest / smallest of those on_c.  Any sphere,
+// any other normal, or the built-in sphere leave the box off.
+static void set_clear_box(SceneDesc &d, const pbf_boundary_t *b)
+{
+    d.clear_box = 0;
+    for (int c = 0; c < 3; ++c) {
+        d.box_lo[c] = -INFINITY;
+        d.box_hi[c] = INFINITY;
+    }
+    if (!b || b->n_inner || b->n_outer) return;
+    for (uint32_t k = 0; k < b->n_planes; ++k) {
+        const float4 on = b->prims[2 * k], n = b->prims[2 * k + 1];
+        const float nc[3] = {n.x, n.y, n.z}, oc[3] = {on.x, on.y, on.z};
+        int axis = -1, zeros = 0;
+        for (int c = 0; c < 3; ++c) {
+            if (nc[c] == 0.f) ++zeros;
+            else if (nc[c] == 1.f || nc[c] == -1.f) axis = c;
+        }
+        if (zeros != 2 || axis < 0) return;
+        if (nc[axis] > 0.f) d.box_lo[axis] = std::max(d.box_lo[axis], oc[axis]);
+        else d.box_hi[axis] = std::min(d.box_hi[axis], oc[axis]);
+    }
+    d.clear_box = 1;
+}
+
 pbf_status Batch::add_scene(const pbf_params &p, uint32_t capacity, const float domain_end[3],
                             const pbf_boundary_t *b, const float amin[3], const float amax[3], const float *x,
                             const float *v, uint32_t n, bool src_dev, cudaStream_t st, uint32_t *id)
@@ -330,6 +359,7 @@ pbf_status Batch::add_scene(const pbf_params &p, uint32_t capacity, const float 
     sh.desc.n_inner = b ? b->n_inner : 0;
     sh.desc.n_outer = b ? b->n_outer : 0;
     sh.desc.n_planes = b ? b->n_planes : 0;
+    set_clear_box(sh.desc, b);
     for (int c = 0; c < 3; ++c) {
         sh.desc.amin[c] = amin[c];
         sh.desc.amax[c] = amax[c];
@@ -527,9 +557,12 @@ pbf_status Batch::set_scene_params(uint32_t id, const pbf_params &p)
     d.n_inner = s.desc.n_inner;
     d.n_outer = s.desc.n_outer;
     d.n_planes = s.desc.n_planes;
+    d.clear_box = s.desc.clear_box;
     for (int c = 0; c < 3; ++c) {
         d.amin[c] = s.desc.amin[c];
         d.amax[c] = s.desc.amax[c];
+        d.box_lo[c] = s.desc.box_lo[c];
+        d.box_hi[c] = s.desc.box_hi[c];
     }
     s.desc = d;
     s.params = p;
@@ -549,6 +582,8 @@ pbf_status Batch::set_scene_boundary(uint32_t id, const pbf_boundary_t *b)
         if (!balloc_.alloc(prims.size(), &bo)) {
             s.bnd_len = 0;
             s.desc.builtin_sphere = 1;
+            s.desc.n_inner = s.desc.n_outer = s.desc.n_planes = 0;
+            set_clear_box(s.desc, nullptr);
             return PBF_ERROR_OUT_OF_MEMORY;
         }
         s.bnd_off = bo;
@@ -560,6 +595,7 @@ pbf_status Batch::set_scene_boundary(uint32_t id, const pbf_boundary_t *b)
     s.desc.n_inner = b ? b->n_inner : 0;
     s.desc.n_outer = b ? b->n_outer : 0;
     s.desc.n_planes = b ? b->n_planes : 0;
+    set_clear_box(s.desc, b);
     dirty_desc_ = true;
     dirty_bnd_ = true;
     return PBF_SUCCESS;

@@ -7,7 +7,7 @@
 
 namespace pbf103 {
 
-// Per-scene constants, one 208-byte record per scene slot in device memory.
+// Per-scene constants, one 224-byte record per scene slot in device memory.
 // Derived once on the host from pbf_params (the reference keeps these in
 // __constant__ symbols and a function-static, pbf_position_update.cu:14-17,
 // pbf_solve.cpp:92; here they are per scene so scenes never share state).
@@ -53,7 +53,10 @@ struct SceneDesc {
     float tens_c;        // reference s_corr: 10 / W(0.4h)^4, the factor of W^4
     float scorr_c;       // textbook s_corr: k / W(dq h)^n, the factor of W^n
     uint32_t list16;     // the neighbour list holds u16 scene-local indices (capacity <= 65,536)
-    uint32_t pad0, pad1, pad2;
+    // clear_box: the boundary is planes with unit-axis normals only; a
+    // projected position p with box_lo <= p <= box_hi hits none of them
+    uint32_t clear_box;
+    float box_lo[3], box_hi[3];
 };
 static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
 

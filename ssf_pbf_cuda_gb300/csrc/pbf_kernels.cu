@@ -228,6 +228,12 @@ __device__ __forceinline__ void plane(bool &hit, float3 &dp, float3 o, float3 p,
 // there with the same dp and the same result.
 __device__ bool collide(const SceneDesc &d, const float4 *__restrict__ bnd, float3 x, float3 &dp)
 {
+    if (d.clear_box) {  // a box's walls: a position inside the clear box hits none, so pass 1 is the last
+        const float px = x.x + dp.x, py = x.y + dp.y, pz = x.z + dp.z;
+        if (d.box_lo[0] <= px && px <= d.box_hi[0] && d.box_lo[1] <= py && py <= d.box_hi[1] &&
+            d.box_lo[2] <= pz && pz <= d.box_hi[2])
+            return true;
+    }
     for (uint32_t pass = 0; pass < d.max_coll; ++pass) {
         const float3 before = dp;
         float3 p = make_float3(x.x + dp.x, x.y + dp.y, x.z + dp.z);
