@@ -168,8 +168,8 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
 
 uint64_t bytes_per_particle(uint32_t max_pair)
 {
-    // x v xs xa xb xold w vt wx (float4) + key slot tmp perm id id_tmp wpos + lam + nnb + cls + nbr
-    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 16ull * ((max_pair - 1 + 3) / 4);  // list slots in whole quads
+    // x v xs xa xb xold w vt wx (float4) + key slot tmp perm id id_tmp wpos + lam + nnb + selfat + cls + nbr
+    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 1 + 16ull * ((max_pair - 1 + 3) / 4);  // list slots in whole quads
 }
 
 // ---------------------------------------------------------------- batch --
@@ -181,7 +181,7 @@ Batch::~Batch()
     if (h_small_) cudaFreeHost(h_small_);
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
-                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
+                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_self_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
                     d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_, d_mid_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -228,6 +228,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_lam_, 4 * P));
     CK(A((void **)&d_nbr_, 16ull * ((max_pair - 1 + 3) / 4) * P));  // quads of 4 slots per particle
     CK(A((void **)&d_nnb_, P));
+    CK(A((void **)&d_self_, P));
     CK(A((void **)&d_cls_, P));
     CK(A((void **)&d_dense_, 4 * (2 * (P / 64 + 1) + 1)));  // a dense bucket holds more than 64 particles
     CK(A((void **)&d_mid_, 4 * (2 * (P / 16 + 1) + 1)));    // a medium one more than 16
@@ -243,6 +244,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(cudaMemset(d_next_id_, 0, 4ull * max_scenes));
     CK(cudaMemset(d_ctrl_, 0, sizeof(Ctrl)));
     CK(cudaMemset(d_nnb_, 0, P));
+    CK(cudaMemset(d_self_, kNotListed, P));
     CK(cudaMemset(d_v_, 0, 16 * P));
     CK(cudaMemset(d_x_, 0, 16 * P));
     CK(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
@@ -754,6 +756,7 @@ StepArgs Batch::args() const
     a.lam = d_lam_;
     a.nbr = d_nbr_;
     a.nnb = d_nnb_;
+    a.selfat = d_self_;
     a.w = d_w_;
     a.vt = d_vt_;
     a.bnd = d_bnd_;
@@ -1023,11 +1026,19 @@ pbf_status Batch::get_debug(uint32_t id, uint32_t *sorted_hash, uint32_t *perm, 
         const uint32_t mp = d.cap + 1;
         const uint64_t padded = ((uint64_t)live + 31) / 32 * 32;
         std::fill(neighbor_list, neighbor_list + padded * mp, 0xFFFFFFFFu);
-        std::vector<uint8_t> nn(live);
+        std::vector<uint8_t> nn(live), self(live);
         std::vector<uint32_t> quads(4ull * live);
-        if (live) CK(cudaMemcpy(nn.data(), d_nnb_ + d.p_off, live, cudaMemcpyDeviceToHost));
+        if (live) {
+            CK(cudaMemcpy(nn.data(), d_nnb_ + d.p_off, live, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(self.data(), d_self_ + d.p_off, live, cudaMemcpyDeviceToHost));
+        }
+        auto at = [&](uint32_t k, uint32_t p) -> uint32_t & {
+            return neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp];
+        };
         // rows of 16 bytes per particle: quads of 4 u32 sorted slots, or
-        // octs of 8 u16 scene-local indices (scenes of at most kList16Max slots)
+        // octs of 8 u16 scene-local indices (scenes of at most kList16Max
+        // slots).  Stored entry k is list slot k, or k + 1 from the particle's
+        // own position on (the particle itself is listed but not stored).
         const uint32_t per_row = d.list16 ? 8u : 4u;
         for (uint32_t kq = 0; per_row * kq < d.cap && live; ++kq) {  // slots per_row*kq.. of every particle
             CK(cudaMemcpy(quads.data(), d_nbr_ + 4ull * ((uint64_t)kq * max_particles_ + d.p_off), 16ull * live,
@@ -1036,9 +1047,11 @@ pbf_status Batch::get_debug(uint32_t id, uint32_t *sorted_hash, uint32_t *perm, 
             for (uint32_t k = per_row * kq; k < per_row * kq + per_row && k < d.cap; ++k)
                 for (uint32_t p = 0; p < live; ++p)
                     if (k < nn[p])
-                        neighbor_list[((uint64_t)k << 5) + (p & 31) + (uint64_t)((p >> 5) << 5) * mp] =
+                        at(k + (k >= self[p] ? 1u : 0u), p) =
                             d.list16 ? octs[8ull * p + (k & 7)] : quads[4ull * p + (k & 3)] - d.p_off;
         }
+        for (uint32_t p = 0; p < live; ++p)
+            if (self[p] != kNotListed) at(self[p], p) = p;
     }
     return PBF_SUCCESS;
 }

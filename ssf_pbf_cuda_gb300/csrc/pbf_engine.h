@@ -141,6 +141,7 @@ private:
     float *d_lam_ = nullptr;
     uint32_t *d_nbr_ = nullptr;
     uint8_t *d_nnb_ = nullptr;
+    uint8_t *d_self_ = nullptr;  // walk-order position of each particle in its own list
     float4 *d_bnd_ = nullptr;
     uint32_t *d_pack_off_ = nullptr;  // per-scene packed offsets for set_all/get_all
     uint32_t *d_id_ = nullptr, *d_id_tmp_ = nullptr;  // particle ids, phase order / sorted scratch

@@ -83,7 +83,8 @@ struct StepArgs {
     float4 *xa, *xb, *xold;       // working positions (ping-pong) and sorted old x
     float *lam;
     uint32_t *nbr;                // nbr[k * nbr_stride + i]
-    uint8_t *nnb;
+    uint8_t *nnb;                 // list entries stored (the particle itself is not stored)
+    uint8_t *selfat;              // position of the particle itself in its walk-order list, kNotListed if cut
     float4 *w, *vt;               // vorticity, XSPH velocity scratch
     const float4 *bnd;            // boundary primitives
     uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
@@ -178,5 +179,6 @@ constexpr uint32_t kCellTileMin = 64, kCellTileMax = 512;  // the autotuner's ra
 constexpr uint32_t kMidMin = 16;            // buckets with more members are queued (warp or block per bucket)
 constexpr uint32_t kSmallStep = 131072;     // particle slots up to which a step is latency bound
 constexpr uint32_t kList16Max = 65536;      // scenes of at most this many slots keep u16 neighbour lists
+constexpr uint8_t kNotListed = 0xFF;        // selfat of a particle the cap cut from its own list
 
 }  // namespace pbf103

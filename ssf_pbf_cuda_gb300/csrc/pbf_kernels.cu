@@ -1125,8 +1125,16 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // group is tested first (independent chains), then the accepted ones are
     // appended in order up to the cap, so the first `cap` accepted ones are
     // the reference's.
+    // The particle itself is accepted (r^2 = 0) and counts toward the cap at
+    // its walk position, but the list does not store it: its pair terms are
+    // W(0) = alpha in the density sum and exactly 0 everywhere else.  selfat
+    // records the position (the debug getter's reference-layout list puts it
+    // back), and the lambda sums start from alpha.  SMEM: the walk collects
+    // every accepted candidate, the particle's own slot is found in shared
+    // memory afterwards and left out of the write-out, so the candidate loop
+    // carries no extra state; otherwise the walk skips it as it stores.
     constexpr uint32_t kNbFetch = 4;
-    uint32_t cnt = 0;
+    uint32_t cnt = 0, selfat = kNotListed;
     walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
                        [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
@@ -1140,12 +1148,17 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
             for (uint32_t k = 0; k < kNbFetch; ++k) {
                 if (acc[k] && cnt < cap) {
                     const uint32_t q = __float_as_uint(c[k].w);
-                    if (SMEM)
+                    if (SMEM) {
                         s_list[cnt * blockDim.x + threadIdx.x] = q;
-                    else if (l16)
-                        nl16[list16_slot(cnt, stride)] = (uint16_t)(q - d.p_off);
-                    else
-                        nl[list_slot(cnt, stride)] = q;
+                    } else {
+                        const uint32_t ks = cnt - (selfat < cnt ? 1u : 0u);  // stored entries before this one
+                        if (q == i)
+                            selfat = cnt;
+                        else if (l16)
+                            nl16[list16_slot(ks, stride)] = (uint16_t)(q - d.p_off);
+                        else
+                            nl[list_slot(ks, stride)] = q;
+                    }
                     ++cnt;
                 }
             }
@@ -1153,23 +1166,33 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
         }
         return true;
     });
+    const uint32_t *rd = s_list + threadIdx.x;
+    if (SMEM) {
+        for (uint32_t k = 0; k < cnt; ++k)
+            if (rd[k * blockDim.x] == i) selfat = k;
+    }
+    cnt -= selfat < cnt ? 1u : 0u;  // entries stored
     a.nnb[i] = (uint8_t)cnt;
+    a.selfat[i] = (uint8_t)selfat;
     // phase 2: lambda over the list just written (L2-resident; plain loads,
     // the read-only path may not see this kernel's own stores)
     LamSum ls;
+    if (selfat != kNotListed) ls.ks = d.alpha;
     if (SMEM) {  // the list from shared memory, written out slot by slot as it is summed
+        // stored entry k is shared-memory entry k, or k + 1 from the
+        // particle's own slot on
+        auto src = [&](uint32_t k) { return rd[(k + (k >= selfat ? 1u : 0u)) * blockDim.x]; };
         // the list out in whole quads (u32) or octs (u16): one 16-byte store
         // per four or eight slots (slots past the count in the last one are
         // padding, never read)
-        const uint32_t *rd = s_list + threadIdx.x;
         uint4 *wq = reinterpret_cast<uint4 *>(nl);
         if (l16) {
             for (uint32_t k0 = 0; k0 < cnt; k0 += 8) {
                 uint32_t w[4];
 #pragma unroll
                 for (uint32_t j = 0; j < 4; ++j) {
-                    const uint32_t lo = (k0 + 2 * j < cnt) ? rd[(k0 + 2 * j) * blockDim.x] - d.p_off : 0u;
-                    const uint32_t hi = (k0 + 2 * j + 1 < cnt) ? rd[(k0 + 2 * j + 1) * blockDim.x] - d.p_off : 0u;
+                    const uint32_t lo = (k0 + 2 * j < cnt) ? src(k0 + 2 * j) - d.p_off : 0u;
+                    const uint32_t hi = (k0 + 2 * j + 1 < cnt) ? src(k0 + 2 * j + 1) - d.p_off : 0u;
                     w[j] = (lo & 0xFFFFu) | (hi << 16);
                 }
                 list_st(wq + (uint64_t)(k0 >> 3) * stride, make_uint4(w[0], w[1], w[2], w[3]));
@@ -1178,16 +1201,12 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
             for (uint32_t k0 = 0; k0 < cnt; k0 += 4) {
                 uint32_t q4[4];
 #pragma unroll
-                for (uint32_t j = 0; j < 4; ++j) q4[j] = (k0 + j < cnt) ? rd[(k0 + j) * blockDim.x] : 0u;
+                for (uint32_t j = 0; j < 4; ++j) q4[j] = (k0 + j < cnt) ? src(k0 + j) : 0u;
                 list_st(wq + (uint64_t)(k0 >> 2) * stride, make_uint4(q4[0], q4[1], q4[2], q4[3]));
             }
         }
 #pragma unroll 4
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t q = *rd;
-            rd += blockDim.x;
-            lam_add(ls, xp, __ldg(xa + q), pc);
-        }
+        for (uint32_t k = 0; k < cnt; ++k) lam_add(ls, xp, __ldg(xa + src(k)), pc);
     } else {
 #pragma unroll 4
         for (uint32_t k = 0; k < cnt; ++k) {
@@ -1243,12 +1262,13 @@ __device__ __forceinline__ uint32_t split_index(const uint32_t *nl, uint64_t str
 template <bool RO>
 __device__ __forceinline__ LamSum lam_sum_split(const uint32_t *nl, uint64_t stride, uint32_t nn,
                                                 const float4 *__restrict__ xc, float4 xp, const SceneDesc &d,
-                                                uint32_t sub, uint32_t gmask)
+                                                uint32_t sub, uint32_t gmask, bool self_listed)
 {
     const PairConst pc = pair_const(d);
     const bool l16 = d.list16 != 0;
     const uint32_t base = d.p_off;
     LamSum ls;
+    if (self_listed) ls.ks = d.alpha;  // the particle's own W(0), first as in the one-lane passes
     float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub, l16, base));
     uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit, l16, base);
     for (uint32_t k0 = 0; k0 < nn; k0 += kSplit) {
@@ -1310,14 +1330,19 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
         int rr0 = sub == 0 ? 0 : 9, rr1 = 9;
         if (!one) split_rows(sub, rr0, rr1);
         uint32_t buf[kSplitCap];
-        uint32_t cnt = 0;
+        // cnt: candidates this lane accepted, the particle itself included
+        // (it counts toward the cap at its walk position but is not stored;
+        // tself is its place in this lane's run)
+        uint32_t cnt = 0, tself = kNotListed;
         if (one && sub == 0) {  // write straight into the list
             walk27_cells<true>(d, a.offsets, a.chist, xa, wx, shift, xp,
                                [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
                 for (uint32_t q = st; q < en; ++q) {
                     const float4 c = __ldg(src + q);
                     if (dist2_exact(xp, c) < h2) {
-                        put(cnt, __float_as_uint(c.w));
+                        const uint32_t qs = __float_as_uint(c.w);
+                        if (qs == i) tself = cnt;
+                        else put(cnt - (tself < cnt ? 1u : 0u), qs);
                         if (++cnt == cap) return false;
                     }
                 }
@@ -1336,7 +1361,9 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
 #pragma unroll
                     for (uint32_t k = 0; k < 4; ++k) {
                         if (acc[k] && cnt < cap) {
-                            buf[cnt] = __float_as_uint(c[k].w);
+                            const uint32_t qs = __float_as_uint(c[k].w);
+                            if (qs == i) tself = cnt;
+                            buf[cnt] = qs;
                             ++cnt;
                         }
                     }
@@ -1353,16 +1380,25 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
             if (sub >= o) incl += v;
         }
         const uint32_t total = __shfl_sync(gmask, incl, kSplit - 1, kSplit);
+        const uint32_t pre = incl - cnt;
+        // the particle's own place in the group's list (one lane holds it)
+        uint32_t gself = tself != kNotListed ? pre + tself : 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t o = 1; o < kSplit; o <<= 1) gself = min(gself, __shfl_xor_sync(gmask, gself, o, kSplit));
+        const bool listed = gself < cap;
         if (!one) {
-            const uint32_t pre = incl - cnt;
-            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) put(pre + t, buf[t]);
+            for (uint32_t t = 0; t < cnt && pre + t < cap; ++t) {
+                const uint32_t g = pre + t;
+                if (g != gself) put(g - (g > gself ? 1u : 0u), buf[t]);
+            }
         }
-        const uint32_t nn = total < cap ? total : cap;
+        const uint32_t nn = (total < cap ? total : cap) - (listed ? 1u : 0u);
         __syncwarp(gmask);  // the list entries of the group are visible to all its lanes
         // lambda of iteration 0 over the list, split over the group's lanes
-        const LamSum ls = lam_sum_split<false>(nl, stride, nn, xa, xp, d, sub, gmask);
+        const LamSum ls = lam_sum_split<false>(nl, stride, nn, xa, xp, d, sub, gmask, listed);
         if (sub == 0) {
             a.nnb[i] = (uint8_t)nn;
+            a.selfat[i] = listed ? (uint8_t)gself : kNotListed;
             a.lam[i] = ls.lambda(d);
         }
     }
@@ -1384,6 +1420,7 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const PairConst pc = pair_const(d);
     const float4 xp = xc[i];
     LamSum ls;
+    if (a.selfat[i] != kNotListed) ls.ks = d.alpha;  // the particle's own W(0), not stored in the list
     list_walk_any<kChunk>(d.list16 != 0, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off,
                           [&](uint32_t q) { lam_add(ls, xp, __ldg(xc + q), pc); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
