@@ -149,11 +149,17 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
     d->inv_wdq = wdq > 0.f ? 1.f / wdq : 0.f;
     d->scorr_k = p.scorr_k;
     d->scorr_n = p.scorr_n;
-    // the pair passes evaluate s_corr as a constant times a power of W:
-    // 10 W^4 / W(0.4h)^4 and k (W / W(dq h))^n = (k / W(dq h)^n) W^n
+    // the pair passes sum t^3 = W / alpha and s' d = grad W / beta and
+    // evaluate s_corr as a constant times a power of t^3:
+    // 10 W^4 / W(0.4h)^4 = (10 alpha^4 / W(0.4h)^4) (t^3)^4 and
+    // k (W / W(dq h))^n = (k alpha^n / W(dq h)^n) (t^3)^n
     d->ih2 = inv_h2;
-    d->tens_c = 10.f * d->inv_k;
-    d->scorr_c = (float)((double)p.scorr_k * std::pow((double)d->inv_wdq, p.scorr_n));
+    const double al = d->alpha, be = d->beta, mr = (double)d->m * (double)d->inv_rho0;
+    d->tens_c = (float)(10.0 * std::pow(al / (double)wpoly6_host(h * 0.4f, inv_h), 4));
+    d->scorr_c = wdq > 0.f ? (float)((double)p.scorr_k * std::pow(al / (double)wdq, p.scorr_n)) : 0.f;
+    d->lam_c = (float)(al * mr);
+    d->lam_k = (float)(mr * mr * be * be);
+    d->dp_k = (float)(mr * be);
     d->tensile_mode = p.tensile_mode;
     d->xsph_mode = p.xsph_mode;
     d->vort_mode = p.vorticity_mode;

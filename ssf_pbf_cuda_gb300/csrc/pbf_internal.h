@@ -7,7 +7,7 @@
 
 namespace pbf103 {
 
-// Per-scene constants, one 224-byte record per scene slot in device memory.
+// Per-scene constants, one 240-byte record per scene slot in device memory.
 // Derived once on the host from pbf_params (the reference keeps these in
 // __constant__ symbols and a function-static, pbf_position_update.cu:14-17,
 // pbf_solve.cpp:92; here they are per scene so scenes never share state).
@@ -50,13 +50,20 @@ struct SceneDesc {
     uint32_t n_planes;
     uint32_t builtin_sphere;
     float ih2;           // 1/h^2 (poly6 from r^2)
-    float tens_c;        // reference s_corr: 10 / W(0.4h)^4, the factor of W^4
-    float scorr_c;       // textbook s_corr: k / W(dq h)^n, the factor of W^n
+    // the pair passes sum W / alpha = t^3 and grad W / beta = s' d (t = 1 -
+    // r^2/h^2, s' = (1 - r/h)^2 / r) and apply alpha and beta once per
+    // particle, through these products (each computed in double):
+    float tens_c;        // reference s_corr: 10 alpha^4 / W(0.4h)^4, the factor of (t^3)^4
+    float scorr_c;       // textbook s_corr: k alpha^n / W(dq h)^n, the factor of (t^3)^n
     uint32_t list16;     // the neighbour list holds u16 scene-local indices (capacity <= 65,536)
     // clear_box: the boundary is planes with unit-axis normals only; a
     // projected position p with box_lo <= p <= box_hi hits none of them
     uint32_t clear_box;
     float box_lo[3], box_hi[3];
+    float lam_c;         // alpha m / rho0: C = lam_c sum t^3 - 1
+    float lam_k;         // m^2 beta^2 / rho0^2: the factor of |sum s' d|^2 + sum (s' r)^2
+    float dp_k;          // m beta / rho0: delta-p = dp_k sum coef s' d
+    uint32_t pad_[1];
 };
 static_assert(sizeof(SceneDesc) % 16 == 0, "SceneDesc must stay 16-byte sized");
 

@@ -66,17 +66,18 @@ __device__ __forceinline__ float dist2_exact(float4 a, float4 b)
 
 // A listed pair at current positions (memorizeKernelPair,
 // src/pbf/solver/cuda/pbf_kernel_memorization.cu:14-56, restated): the
-// difference d = x_i - x_j, r^2, the poly6 value W and the spiky gradient
-// as a factor s of d (grad W = s d):
-//   W = alpha (1 - r^2 / h^2)^3          for r <= h, else 0
-//   s = beta (1 - r / h)^2 / r           for 0 < r <= h, else 0
-//   sr = s r = |grad W| (up to sign)
+// difference d = x_i - x_j, r^2, the poly6 value W = alpha w and the spiky
+// gradient grad W = beta s d, with the scene factors alpha and beta left
+// out of the per-pair terms (the sums apply them once per particle):
+//   w = (1 - r^2 / h^2)^3                for r <= h, else 0
+//   s = (1 - r / h)^2 / r                for 0 < r <= h, else 0
+//   sr = s r = |grad W| / |beta|
 // The clamps replace the reference's branches: 1 - r^2/h^2 and 1 - r/h are
 // clamped at 0 (r > h), and r^2 enters the reciprocal square root no smaller
-// than kMinR2, so the pair of a particle with itself (r^2 = 0, d = 0, r = 0)
-// gets a finite s (up to beta / 1e-15), a gradient s d of exactly 0 and
-// sr = 0, as the reference's r^2 > 0 test gives.  |grad W|^2 is taken as
-// sr^2, not s^2 r^2: the latter overflows for the self pair.
+// than kMinR2, so a pair at distance 0 (d = 0, r = 0) gets a finite s (up
+// to 1e15), a gradient s d of exactly 0 and sr = 0, as the reference's
+// r^2 > 0 test gives.  |grad W|^2 is taken as sr^2, not s^2 r^2: the
+// latter overflows at r = 0.
 // Products and sums are rounded one by one or fused where written
 // (__fmaf_rn), never contracted by the compiler, so every pass that calls
 // these, in one lane or split over lanes, gets the same bits.
@@ -102,28 +103,27 @@ struct PairWS {
 
 // per-scene constants of the pair math, in registers for a particle's loop
 struct PairConst {
-    float ih2, inv_h, alpha, beta;
+    float ih2, inv_h;
 };
 
-__device__ __forceinline__ PairConst pair_const(const SceneDesc &d)
-{
-    return PairConst{d.ih2, d.inv_h, d.alpha, d.beta};
-}
+__device__ __forceinline__ PairConst pair_const(const SceneDesc &d) { return PairConst{d.ih2, d.inv_h}; }
 
 __device__ __forceinline__ PairWS pair_ws(float r2, const PairConst &c)
 {
     const float inv_r = rsqrtf(fmaxf(r2, kMinR2));
     const float t = fmaxf(__fmaf_rn(-r2, c.ih2, 1.f), 0.f);
-    const float W = __fmul_rn(__fmul_rn(c.alpha, t), __fmul_rn(t, t));
+    const float W = __fmul_rn(__fmul_rn(t, t), t);
     const float r = __fmul_rn(r2, inv_r);
     const float u = fmaxf(__fmaf_rn(-r, c.inv_h, 1.f), 0.f);
-    const float s = __fmul_rn(__fmul_rn(c.beta, inv_r), __fmul_rn(u, u));
+    const float s = __fmul_rn(inv_r, __fmul_rn(u, u));
     return PairWS{W, s, __fmul_rn(s, r)};
 }
 
 // The sums of calcScalingFactorCUDA (pbf_constraint.cu:168-209) over a
-// particle's list, added in list order: sum W, sum grad W = sum s d, and
-// sum |grad W|^2 = sum (s r)^2.
+// particle's list, added in list order, without the factors alpha and
+// beta: sum w (W = alpha w), sum s d (grad W = beta s d) and sum (s r)^2.
+// A particle's own pair (w = 1, no gradient) is not stored in its list; the
+// passes start ks at 1 for it.
 struct LamSum {
     float ks = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, kg2 = 0.f;
     __device__ __forceinline__ void add(float W, float s, float d0, float d1, float d2, float sr)
@@ -135,12 +135,13 @@ struct LamSum {
         kg2 = __fmaf_rn(sr, sr, kg2);
     }
     __device__ __forceinline__ void add(const PairGeo &g, const PairWS &k) { add(k.W, k.s, g.d0, g.d1, g.d2, k.sr); }
-    // lambda = C / (m^2 / rho0^2 |grad C|^2 + eps)
+    // lambda = C / (m^2 / rho0^2 |grad C|^2 + eps), with C = alpha m / rho0
+    // sum w - 1 and m^2 / rho0^2 |grad C|^2 = m^2 beta^2 / rho0^2 K
     __device__ __forceinline__ float lambda(const SceneDesc &d) const
     {
-        const float C = __fmaf_rn(__fmul_rn(ks, d.m), d.inv_rho0, -1.f);
+        const float C = __fmaf_rn(ks, d.lam_c, -1.f);
         const float K = __fmaf_rn(g0, g0, __fmaf_rn(g2, g2, __fmaf_rn(g1, g1, kg2)));
-        return __fdiv_rn(C, __fmaf_rn(d.m2rho2, K, d.relax));
+        return __fdiv_rn(C, __fmaf_rn(d.lam_k, K, d.relax));
     }
 };
 
@@ -1127,9 +1128,9 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // the reference's.
     // The particle itself is accepted (r^2 = 0) and counts toward the cap at
     // its walk position, but the list does not store it: its pair terms are
-    // W(0) = alpha in the density sum and exactly 0 everywhere else.  selfat
+    // w(0) = 1 in the density sum and exactly 0 everywhere else.  selfat
     // records the position (the debug getter's reference-layout list puts it
-    // back), and the lambda sums start from alpha.  SMEM: the walk collects
+    // back), and the lambda sums start from 1.  SMEM: the walk collects
     // every accepted candidate, the particle's own slot is found in shared
     // memory afterwards and left out of the write-out, so the candidate loop
     // carries no extra state; otherwise the walk skips it as it stores.
@@ -1177,7 +1178,7 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // phase 2: lambda over the list just written (L2-resident; plain loads,
     // the read-only path may not see this kernel's own stores)
     LamSum ls;
-    if (selfat != kNotListed) ls.ks = d.alpha;
+    if (selfat != kNotListed) ls.ks = 1.f;
     if (SMEM) {  // the list from shared memory, written out slot by slot as it is summed
         // stored entry k is shared-memory entry k, or k + 1 from the
         // particle's own slot on
@@ -1268,7 +1269,7 @@ __device__ __forceinline__ LamSum lam_sum_split(const uint32_t *nl, uint64_t str
     const bool l16 = d.list16 != 0;
     const uint32_t base = d.p_off;
     LamSum ls;
-    if (self_listed) ls.ks = d.alpha;  // the particle's own W(0), first as in the one-lane passes
+    if (self_listed) ls.ks = 1.f;  // the particle's own w(0), first as in the one-lane passes
     float4 x0 = __ldg(xc + split_index<RO>(nl, stride, nn, sub, l16, base));
     uint32_t q1 = split_index<RO>(nl, stride, nn, sub + kSplit, l16, base);
     for (uint32_t k0 = 0; k0 < nn; k0 += kSplit) {
@@ -1420,7 +1421,7 @@ __global__ void __launch_bounds__(512, 2) k_lambda(StepArgs a, float4 *__restric
     const PairConst pc = pair_const(d);
     const float4 xp = xc[i];
     LamSum ls;
-    if (a.selfat[i] != kNotListed) ls.ks = d.alpha;  // the particle's own W(0), not stored in the list
+    if (a.selfat[i] != kNotListed) ls.ks = 1.f;  // the particle's own w(0), not stored in the list
     list_walk_any<kChunk>(d.list16 != 0, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off,
                           [&](uint32_t q) { lam_add(ls, xp, __ldg(xc + q), pc); });
     // LAMW: lambda rides in .w of the positions this pass reads and the
@@ -1440,16 +1441,16 @@ enum ScorrForm { kScorrReference, kScorrTextbook, kScorrOff, kScorrTextbook4 };
 
 struct ScorrConst {
     float sci;  // max(-lambda_i, 0), the reference form's own share
-    float c;    // the factor of W^n: 10 / W(0.4h)^4 (reference), k / W(dq h)^n (textbook)
+    float c;    // the factor of w^n: 10 alpha^4 / W(0.4h)^4 (reference), k alpha^n / W(dq h)^n (textbook)
     int sn;
 };
 
 // -(lambda_i + lambda_j + s_corr) for a pair (the coefficient of grad W in
 // calcPositionUpdateCUDA, pbf_position_update.cu:131-188).  s_corr as a
-// constant times a power of W: reference 10 W^4 / W(0.4h)^4 (max(-lambda_i,
-// 0) + max(-lambda_j, 0)) (pbf_position_update.cu:136-146), textbook
-// k (W / W(dq h))^n (Macklin and Mueller 2013, eq. 13); its last product is
-// fused into the sum.
+// constant times a power of w = W / alpha: reference 10 W^4 / W(0.4h)^4
+// (max(-lambda_i, 0) + max(-lambda_j, 0)) (pbf_position_update.cu:136-146),
+// textbook k (W / W(dq h))^n (Macklin and Mueller 2013, eq. 13); its last
+// product is fused into the sum.
 template <int FORM>
 __device__ __forceinline__ float dp_coef(float li, float lj, float W, const ScorrConst &c)
 {
@@ -1507,7 +1508,7 @@ __device__ __forceinline__ float3 dp_sum(const StepArgs &a, const SceneDesc &d, 
 __device__ __forceinline__ void dp_finish(const StepArgs &a, const SceneDesc &d, uint32_t s, uint32_t i, float4 xp,
                                           float3 sum, float4 *__restrict__ xo, float4 *__restrict__ vo, int last)
 {
-    float3 dp = make_float3(sum.x * d.m * d.inv_rho0, sum.y * d.m * d.inv_rho0, sum.z * d.m * d.inv_rho0);
+    float3 dp = make_float3(sum.x * d.dp_k, sum.y * d.dp_k, sum.z * d.dp_k);  // m beta / rho0
     const bool ok = collide(d, a.bnd, make_float3(xp.x, xp.y, xp.z), dp);
     if (!ok) atomicOr(a.flags + s, PBF_FLAG_COLLISION_LIMIT);
     const float4 xn = make_float4(xp.x + dp.x, xp.y + dp.y, xp.z + dp.z, 0.f);
