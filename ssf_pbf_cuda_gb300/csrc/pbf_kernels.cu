@@ -357,8 +357,8 @@ __device__ __forceinline__ void walk27_cells(const SceneDesc &d, const uint32_t 
             const uint32_t b = row + ((uint32_t)tx & (d.gx - 1u));
             uint32_t st = __ldg(off + b);
             uint32_t en = __ldg(off + b + 1);
-            if (st == en) continue;
             const uint64_t h = __ldg(reinterpret_cast<const unsigned long long *>(ch + b));
+            if (st == en) continue;
             const float4 *src = xa;
             if (h != kClassWhole) {
                 const uint32_t sh = 8u * (cyz | (uint32_t)((tx >> sx) & 1));
@@ -475,7 +475,10 @@ __device__ __forceinline__ uint32_t oct_at(const uint4 &v, int j)
 }
 
 // list_walk over a u16 list: octs requested one chunk (8 slots) ahead;
-// f gets base + the scene-local index, i.e. the particle's sorted slot.
+// f gets base + the scene-local index: the particle's sorted slot for base
+// = the scene's first slot, the scene-local index itself for base = 0 (for
+// arrays offset by the scene's first slot, which saves the add per slot;
+// measured faster in the XSPH and vorticity-apply passes only).
 template <class F>
 __device__ __forceinline__ void list_walk16(const uint32_t *__restrict__ nl, uint64_t stride, uint32_t nn,
                                             uint32_t base, F &&f)
@@ -1643,7 +1646,8 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
     const float sgn = REF ? 1.f : -1.f;
     const float4 *__restrict__ x = a.x;
     const float4 *__restrict__ w = a.w;
-    const float4 *__restrict__ xw = a.xs;  // (x_j, |omega_j|), stored by pass 1
+    const uint32_t lb = (!REF && L16) ? d.p_off : 0u;  // use(j): j counts from lb
+    const float4 *__restrict__ xw = a.xs + lb;          // (x_j, |omega_j|), stored by pass 1
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
     auto use = [&](uint32_t j) {
         const float4 xj = __ldg(xw + j);
@@ -1669,7 +1673,7 @@ __global__ void __launch_bounds__(512) k_vort_apply(StepArgs a, float4 *__restri
             use);
     } else {
         // quads of 4: fewer registers, more warps (measured)
-        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
+        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], 0u, use);
     }
     const float4 wi = w[i];
     const float mr = d.m * d.inv_rho0;
@@ -1723,17 +1727,20 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
     }
     const float inv_h = d.inv_h, alpha6 = d.alpha6;
     const float4 *__restrict__ x = a.x;
+    const uint32_t lb = (!WALK && L16) ? d.p_off : 0u;  // use(j): j counts from lb
+    const float4 *__restrict__ xb = x + lb;
+    const float4 *__restrict__ vb = vs + lb;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     const float ih2 = inv_h * inv_h;
     auto use = [&](uint32_t j) {
-        const float4 xj = __ldg(x + j);
+        const float4 xj = __ldg(xb + j);
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
         // Wpoly6 from r^2 (q^2 = r^2 / h^2 instead of (|r| / h)^2: no square
         // root per pair; the two differ by rounding only)
         const float q2 = (p0 * p0 + p1 * p1 + p2 * p2) * ih2;
         const float t = 1.f - q2;
         const float W = (q2 <= 1.f) ? alpha6 * t * t * t : 0.f;
-        const float4 vj = __ldg(vs + j);
+        const float4 vj = __ldg(vb + j);
         s0 += (vj.x - vi.x) * W;
         s1 += (vj.y - vi.y) * W;
         s2 += (vj.z - vi.z) * W;
@@ -1753,7 +1760,7 @@ __global__ void __launch_bounds__(512) k_xsph(StepArgs a, const float4 *__restri
             use);
     } else {
         if (L16)
-            list_walk16(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
+            list_walk16(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], 0u, use);
         else
             list_walk_ahead2(list_of(a.nbr, i), a.nbr_stride, a.nnb[i], use);
     }
