@@ -636,7 +636,12 @@ def main():
                 "kernel_share": {k: v / sum(tot_by_kernel.values()) for k, v in
                                  sorted(tot_by_kernel.items(), key=lambda kv: -kv[1])},
                 "kernel_ms_per_launch": {k: round(m, 5) for k, (m, _) in
-                                         sorted(per_kernel.items(), key=lambda kv: -kv[1][0] * kv[1][1])}}
+                                         sorted(per_kernel.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
+                # every kernel with algorithmic bytes: the same fraction of the peak
+                "kernel_frac": {k: round((ALG_KERNEL[k][0] * n_total + ALG_KERNEL[k][1] * cells) /
+                                         (m / 1e3) / 1e9 / peak, 4)
+                                for k, (m, _) in sorted(per_kernel.items(), key=lambda kv: -kv[1][0] * kv[1][1])
+                                if k in ALG_KERNEL}}
 
     # ---------------- e2e through the C ABI with host buffers ----------------
     e2e = None
