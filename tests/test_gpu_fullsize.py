@@ -176,3 +176,43 @@ def test_large_step_list_slots(oracle, gpu, max_pair):
     g = H.run_gpu(sc, params, "planes", iters=1)
     r = H.run_oracle(oracle, sc, params, "planes", iters=1)
     H.assert_integer_parity(g, r, H.resolved(params, sc))
+
+
+def _dense_cells_scene():
+    """140,000 particles: 20,000 packed into eight cells (2,500 a cell, so
+    buckets above 255 members, walked whole, and cells of far more than 32
+    particles), the rest uniform over the box."""
+    rng = np.random.default_rng(123)
+    k = np.arange(20000) % 8
+    corner = np.stack([(k & 1) * 0.1, ((k >> 1) & 1) * 0.1, ((k >> 2) & 1) * 0.1], axis=1) + 1.2
+    dense = corner + rng.uniform(0.005, 0.095, size=(20000, 3))
+    rest = rng.uniform(0.05, 3.15, size=(120000, 3))
+    x = np.concatenate([dense, rest]).astype(np.float32)
+    return scenes.Scene(x, np.zeros_like(x), (3.2, 3.2, 3.2), ((-0.1,) * 3, (3.3,) * 3),
+                        scenes.box_planes((3.2, 3.2, 3.2)), grid=(16, 16, 16))
+
+
+HARD_TABLES = {
+    # buckets mixing up to 8 alias classes (cells 16 apart share a bucket)
+    "aliased": lambda: scenes.dam_break(64, 48, 48, (8.0, 4.0, 4.0), scene_id=131, grid=(16, 16, 16)),
+    # 2 cells on x: every bucket walked whole, wrapped buckets visited twice
+    "small_axes": lambda: scenes.dam_break(64, 48, 48, (8.0, 4.0, 4.0), scene_id=132, grid=(2, 16, 16)),
+    "dense_cells": _dense_cells_scene,
+}
+
+
+@pytest.mark.parametrize("case", sorted(HARD_TABLES))
+def test_large_step_lists_on_hard_tables(oracle, gpu, case):
+    """Large steps (over 131,072 particle slots: the per-cell rank, the
+    one-lane walk) on hard tables: buckets mixing alias classes (walked
+    through the class-grouped walk copy), an axis of 2 cells (buckets
+    walked whole, wrapped cells visited twice, 64 list slots so the
+    duplicates fit), and cells of 2,500 particles (buckets of more than 255
+    members, walked whole; every list capped).  Hashes, permutation, cell
+    ranges and lists equal the oracle's slot for slot."""
+    sc = HARD_TABLES[case]()
+    assert sc.n > 131072
+    params = api.config_params(scorr_k=1e-4, max_pair_particle_num=64 if case == "small_axes" else 30)
+    g = H.run_gpu(sc, params, "planes", iters=0)
+    r = H.run_oracle(oracle, sc, params, "planes", iters=0)
+    H.assert_integer_parity(g, r, H.resolved(params, sc))
