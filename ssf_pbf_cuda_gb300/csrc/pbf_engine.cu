@@ -225,7 +225,9 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_flags_, 4ull * max_scenes));
     CK(A((void **)&d_next_id_, 4ull * max_scenes));
     float4 **f4[] = {&d_x_, &d_v_, &d_xs_, &d_xa_, &d_xb_, &d_xold_, &d_w_, &d_vt_, &d_wx_};
-    for (float4 **p : f4) CK(A((void **)p, 16 * P));
+    // + kWalkSpare records: the neighbour walk reads candidates in groups of
+    // four and may read up to three past the end of a range (never accepted)
+    for (float4 **p : f4) CK(A((void **)p, 16 * (P + kWalkSpare)));
     uint32_t **u4[] = {&d_key_, &d_slot_, &d_tmp_, &d_perm_, &d_id_, &d_id_tmp_, &d_wpos_};
     for (uint32_t **p : u4) CK(A((void **)p, 4 * P));
     CK(A((void **)&d_count_, 4 * (C + 4)));

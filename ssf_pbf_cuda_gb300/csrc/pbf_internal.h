@@ -187,5 +187,6 @@ constexpr uint32_t kMidMin = 16;            // buckets with more members are que
 constexpr uint32_t kSmallStep = 131072;     // particle slots up to which a step is latency bound
 constexpr uint32_t kList16Max = 65536;      // scenes of at most this many slots keep u16 neighbour lists
 constexpr uint8_t kNotListed = 0xFF;        // selfat of a particle the cap cut from its own list
+constexpr uint32_t kWalkSpare = 4;          // spare float4 records after each per-particle array
 
 }  // namespace pbf103

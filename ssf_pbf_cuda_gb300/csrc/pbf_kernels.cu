@@ -1125,7 +1125,9 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
     // different candidates, so pair math inside the walk would run masked
     // for almost every candidate); a candidate's .w is its sorted slot
     // Candidates are fetched kNbFetch at a time (more loads in flight; a
-    // group past the range's end re-reads its last candidate), all of the
+    // group past the range's end reads up to kNbFetch - 1 records beyond it,
+    // never accepted: xa and wx carry that many spare records at the end of
+    // their allocations), all of the
     // group is tested first (independent chains), then the accepted ones are
     // appended in order up to the cap, so the first `cap` accepted ones are
     // the reference's.
@@ -1143,8 +1145,9 @@ __global__ void __launch_bounds__(512, 2) k_neighbors_lambda(StepArgs a)
                        [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
         for (uint32_t q0 = st; q0 < en; q0 += kNbFetch) {
             float4 c[kNbFetch];
+            const float4 *pq = src + q0;
 #pragma unroll
-            for (uint32_t k = 0; k < kNbFetch; ++k) c[k] = __ldg(src + min(q0 + k, en - 1u));
+            for (uint32_t k = 0; k < kNbFetch; ++k) c[k] = __ldg(pq + k);
             bool acc[kNbFetch];
 #pragma unroll
             for (uint32_t k = 0; k < kNbFetch; ++k) acc[k] = (q0 + k < en) && dist2_exact(xp, c[k]) < h2;
@@ -1357,8 +1360,9 @@ __global__ void __launch_bounds__(256) k_neighbors_split(StepArgs a, uint32_t ti
                                [&](const float4 *src, uint32_t st, uint32_t en) -> bool {
                 for (uint32_t q0 = st; q0 < en; q0 += 4) {
                     float4 c[4];
+                    const float4 *pq = src + q0;  // up to three spare records past the range
 #pragma unroll
-                    for (uint32_t k = 0; k < 4; ++k) c[k] = __ldg(src + min(q0 + k, en - 1u));
+                    for (uint32_t k = 0; k < 4; ++k) c[k] = __ldg(pq + k);
                     bool acc[4];
 #pragma unroll
                     for (uint32_t k = 0; k < 4; ++k) acc[k] = (q0 + k < en) && dist2_exact(xp, c[k]) < h2;
