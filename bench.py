@@ -651,7 +651,9 @@ def main():
         # copy stream through device staging buffers (two for the inputs), so
         # step k+1's upload and step k-1's download overlap step k's compute;
         # the compute stream runs pbf_batch_set_all from the staged inputs,
-        # the step and pbf_batch_get_all into the staged outputs.
+        # the step and pbf_batch_get_all_async into the staged outputs (the
+        # packed offsets computed on the device: the host never waits for a
+        # step, only for a staging buffer to come free).
         xh = torch.from_numpy(x0h).pin_memory()
         vh = torch.from_numpy(v0h).pin_memory()
         xo = torch.empty_like(xh).pin_memory()
@@ -660,6 +662,8 @@ def main():
         vin = [torch.empty(vh.shape, dtype=vh.dtype, device=dev) for _ in range(2)]
         xout = torch.empty(xh.shape, dtype=xh.dtype, device=dev)
         vout = torch.empty(vh.shape, dtype=vh.dtype, device=dev)
+        cout = torch.empty(len(counts), dtype=torch.int32, device=dev)
+        co = torch.empty(len(counts), dtype=torch.int32).pin_memory()
         cs = torch.cuda.Stream(dev)
         in_ready = [torch.cuda.Event(), torch.cuda.Event()]
         out_ready, out_free = torch.cuda.Event(), torch.cuda.Event()
@@ -677,10 +681,11 @@ def main():
 
         def download():
             stream.wait_event(out_free)  # the previous download has left the staging buffer
-            batch.get_all(xout, vout, stream)  # waits for the step (live counts), packs on the stream
+            batch.get_all_async(cout, xout, vout, stream)  # packs on the stream, live counts included
             out_ready.record(stream)
             cs.wait_event(out_ready)
             with torch.cuda.stream(cs):
+                co.copy_(cout, non_blocking=True)
                 xo.copy_(xout, non_blocking=True)
                 vo.copy_(vout, non_blocking=True)
                 out_free.record(cs)
@@ -707,12 +712,15 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dt = float(t.item())
         e2e = {"value": job_particles * args.steps / dt, "unit": UNIT,
-               "h2d_bytes_per_step": int(x0h.nbytes + v0h.nbytes), "d2h_bytes_per_step": int(x0h.nbytes + v0h.nbytes),
+               "h2d_bytes_per_step": int(x0h.nbytes + v0h.nbytes),
+               "d2h_bytes_per_step": int(x0h.nbytes + v0h.nbytes + 4 * len(counts)),
                "ms_per_step": dt / args.steps * 1e3,
                "pipeline": "one batch; host->device and device->host copies of pinned buffers on a copy "
                            "stream through device staging, overlapping the neighbouring steps' compute; "
-                           "pbf_batch_set_all / step / get_all on the compute stream"}
-        del xin, vin, xout, vout
+                           "pbf_batch_set_all / step / get_all_async on the compute stream, no host wait "
+                           "on a step"}
+        assert int(co.numpy().view(np.uint32).sum()) > 0
+        del xin, vin, xout, vout, cout
 
     # ---------------- plain: the same scenes one at a time ----------------
     plain = None

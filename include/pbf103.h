@@ -241,6 +241,15 @@ pbf_status pbf_batch_set_all(pbf_batch *b, const uint32_t *counts, const float *
                              int src_is_device, void *stream);
 pbf_status pbf_batch_get_all(pbf_batch *b, uint32_t *counts, float *x, float *v, int dst_is_device,
                              void *stream);
+/* pbf_batch_get_all into device buffers without a host round trip: the
+ * packed offsets are computed on the device from the live counts, so the
+ * call only enqueues work on the stream.  counts_dev[k] (device memory)
+ * receives the k-th active scene's live count; read it once the stream has
+ * reached this point.  x_dev / v_dev (either may be NULL) get the same packed
+ * layout as pbf_batch_get_all and must hold the active scenes' capacities,
+ * since the live counts are not known on the host when the call is made.
+ * No reference counterpart. */
+pbf_status pbf_batch_get_all_async(pbf_batch *b, uint32_t *counts_dev, float *x_dev, float *v_dev, void *stream);
 /* Time candidate launch shapes on the current scenes and keep the fastest.
  * Leaves particle state unchanged. */
 pbf_status pbf_batch_autotune(pbf_batch *b, int iters, void *stream, uint32_t *chosen_tile);

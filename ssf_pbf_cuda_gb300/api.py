@@ -543,6 +543,13 @@ class Batch:
                                        _stream(stream)), "pbf_batch_get_all")
         return counts[:len(ids)], x_out, v_out
 
+    def get_all_async(self, counts_dev, x_dev=None, v_dev=None, stream=None):
+        """Download every active scene into device buffers (packed as get_all)
+        without waiting for the stream: counts_dev (device uint32, one per
+        active scene) receives the live counts once the stream gets there."""
+        check(load().pbf_batch_get_all_async(self.handle, _ptr(counts_dev), _ptr(x_dev), _ptr(v_dev),
+                                             _stream(stream)), "pbf_batch_get_all_async")
+
     def profile_step(self, iters: int, stream=None) -> list:
         """One step without a graph, with CUDA events between kernels; returns
         [(kernel name, milliseconds)] in launch order."""

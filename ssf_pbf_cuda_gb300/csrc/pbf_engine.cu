@@ -187,7 +187,7 @@ Batch::~Batch()
     if (h_small_) cudaFreeHost(h_small_);
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
-                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_self_, d_bnd_, d_pack_off_, d_id_, d_id_tmp_,
+                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_self_, d_bnd_, d_pack_off_, d_active_, d_id_, d_id_tmp_,
                     d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_, d_mid_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -243,6 +243,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_chist_, 8 * (C + 4)));
     CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
     CK(A((void **)&d_pack_off_, 4ull * max_scenes));
+    CK(A((void **)&d_active_, 4ull * max_scenes));
     CK(cudaMallocHost((void **)&h_small_, 8ull * max_scenes + 64));
     CK(cudaEventCreateWithFlags(&small_done_, cudaEventDisableTiming));
     CK(cudaMemset(d_count_, 0, 4 * (C + 4)));
@@ -544,6 +545,18 @@ pbf_status Batch::download_all(uint32_t *counts, float *x, float *v, bool dst_de
     return PBF_SUCCESS;
 }
 
+pbf_status Batch::download_all_async(uint32_t *counts_dev, float *x_dev, float *v_dev, cudaStream_t st)
+{
+    CK(cudaSetDevice(device_));
+    pbf_status rc = upload(st);
+    if (rc != PBF_SUCCESS) return rc;
+    if (n_active_ == 0) return PBF_SUCCESS;
+    launch_pack_offsets(d_active_, n_active_, d_scene_num_, d_pack_off_, counts_dev, st);
+    if (ctrl_.n_tiles && (x_dev || v_dev)) launch_pack(args(), shape_for(tile_), d_pack_off_, x_dev, v_dev, st);
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
 pbf_status Batch::set_scene_params(uint32_t id, const pbf_params &p)
 {
     if (id >= scenes_.size() || !scenes_[id].active) return PBF_ERROR_NOT_FOUND;
@@ -679,6 +692,10 @@ pbf_status Batch::upload(cudaStream_t st)
                                st));
         }
         CK(cudaMemcpyAsync(d_ctrl_, &ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, st));
+        std::vector<uint32_t> ids;
+        scene_ids(ids);
+        n_active_ = (uint32_t)ids.size();
+        if (n_active_) CK(cudaMemcpyAsync(d_active_, ids.data(), 4ull * n_active_, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
         dirty_tiles_ = false;
     }

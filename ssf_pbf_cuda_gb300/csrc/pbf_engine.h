@@ -78,6 +78,9 @@ public:
     void scene_ids(std::vector<uint32_t> &ids) const;
     pbf_status upload_all(const uint32_t *counts, const float *x, const float *v, bool src_dev, cudaStream_t st);
     pbf_status download_all(uint32_t *counts, float *x, float *v, bool dst_dev, cudaStream_t st);
+    // the whole batch into device buffers with the packed offsets computed on
+    // the device: no host synchronisation; counts_dev[k] for the k-th active scene
+    pbf_status download_all_async(uint32_t *counts_dev, float *x_dev, float *v_dev, cudaStream_t st);
     pbf_status import_x_device(uint32_t id, const float *x_dev, uint32_t n, cudaStream_t st);
     // device arrays of one scene, for the particle-set operations (pbf_particles.cu)
     struct SceneArrays {
@@ -144,6 +147,8 @@ private:
     uint8_t *d_self_ = nullptr;  // walk-order position of each particle in its own list
     float4 *d_bnd_ = nullptr;
     uint32_t *d_pack_off_ = nullptr;  // per-scene packed offsets for set_all/get_all
+    uint32_t *d_active_ = nullptr;    // active scene slots in slot order (with the tile lists)
+    uint32_t n_active_ = 0;
     uint32_t *d_id_ = nullptr, *d_id_tmp_ = nullptr;  // particle ids, phase order / sorted scratch
     uint32_t *d_next_id_ = nullptr;                   // per scene: next id to hand out
     uint8_t *d_cls_ = nullptr;                        // alias class per particle (input order)

@@ -160,6 +160,10 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, uint32
 void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st);
 void launch_f4_to_aos3(const float4 *src, float *dst, uint32_t n, cudaStream_t st);
 void launch_set_u32(uint32_t *dst, uint32_t value, cudaStream_t st);
+// pack_off[active[k]] = sum of the live counts of active[0..k), counts[k] =
+// the live count of active[k], computed on the device (one block)
+void launch_pack_offsets(const uint32_t *active, uint32_t n_active, const uint32_t *scene_num, uint32_t *pack_off,
+                         uint32_t *counts, cudaStream_t st);
 // ids of n particles added at dst: append ? *next_id + k : k; *next_id += / = n.
 void launch_assign_ids(uint32_t *dst, uint32_t *next_id, uint32_t n, bool append, cudaStream_t st);
 // Whole-batch moves between a packed AoS float3 buffer (active scenes in

@@ -1860,6 +1860,38 @@ __global__ void __launch_bounds__(512) k_pack(StepArgs a, const uint32_t *__rest
 
 __global__ void k_set_u32(uint32_t *dst, uint32_t value) { *dst = value; }
 
+// Packed offsets of the active scenes from their live counts, on the device:
+// pack_off[active[k]] = the counts of active[0..k) summed, counts[k] = the
+// count of active[k] (k-th active scene in slot order).  One block.
+__global__ void __launch_bounds__(1024) k_pack_offsets(const uint32_t *__restrict__ active, uint32_t n_active,
+                                                       const uint32_t *__restrict__ scene_num,
+                                                       uint32_t *__restrict__ pack_off, uint32_t *__restrict__ counts)
+{
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    if (t == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t k0 = 0; k0 < n_active; k0 += blockDim.x) {
+        const uint32_t k = k0 + t;
+        const uint32_t id = k < n_active ? active[k] : 0u;
+        const uint32_t c = k < n_active ? scene_num[id] : 0u;
+        const uint32_t incl = warp_incl_scan(c);
+        if (lane == 31) ws[warp] = incl;
+        __syncthreads();
+        if (warp == 0) ws[lane] = warp_incl_scan(lane < (blockDim.x >> 5) ? ws[lane] : 0u);
+        __syncthreads();
+        const uint32_t before = carry + (warp ? ws[warp - 1] : 0u) + incl - c;
+        if (k < n_active) {
+            pack_off[id] = before;
+            counts[k] = c;
+        }
+        __syncthreads();
+        if (t == blockDim.x - 1) carry = before + c;
+        __syncthreads();
+    }
+}
+
 __global__ void k_aos3_to_f4(const float *__restrict__ src, float4 *__restrict__ dst, uint32_t n)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1957,6 +1989,12 @@ void launch_f4_to_aos3(const float4 *src, float *dst, uint32_t n, cudaStream_t s
 }
 
 void launch_set_u32(uint32_t *dst, uint32_t value, cudaStream_t st) { k_set_u32<<<1, 1, 0, st>>>(dst, value); }
+
+void launch_pack_offsets(const uint32_t *active, uint32_t n_active, const uint32_t *scene_num, uint32_t *pack_off,
+                         uint32_t *counts, cudaStream_t st)
+{
+    if (n_active) k_pack_offsets<<<1, 1024, 0, st>>>(active, n_active, scene_num, pack_off, counts);
+}
 
 void launch_unpack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_off, const float *src_x,
                    const float *src_v, cudaStream_t st)

@@ -154,6 +154,36 @@ def test_set_all_get_all_roundtrip(gpu):
     assert np.array_equal(x2, x + np.float32(0.001)) and np.array_equal(v2, v + np.float32(0.5))
 
 
+def test_get_all_async_equals_get_all(gpu):
+    """pbf_batch_get_all_async packs the batch into device buffers with the
+    packed offsets computed on the device from the live counts (no host
+    round trip): the same counts and particles as pbf_batch_get_all, with a
+    removed scene's slot left out and a scene whose area deletes a third of
+    its particles in the first step."""
+    import dataclasses
+    import torch
+    items = mixed_scenes()
+    sc = scenes.dam_break(12, 12, 12, (1.5, 1.5, 1.5), scene_id=52)
+    items.append((dataclasses.replace(sc, area=((-0.1, -0.1, -0.1), (1.6, 0.45, 1.6))),
+                  api.config_params(scorr_k=1e-4)))
+    b, ids = make_batch(items)
+    b.remove_scene(ids[1])
+    for _ in range(2):
+        b.step(4)
+    counts, x, v = b.get_all()
+    assert counts[-1] < sc.n  # the last scene lost particles
+    cap = sum(sc_.n for k, (sc_, _) in enumerate(items) if k != 1)
+    cd = torch.zeros(len(counts), dtype=torch.int32, device="cuda")
+    xd = torch.full((cap, 3), -1.0, dtype=torch.float32, device="cuda")
+    vd = torch.full((cap, 3), -1.0, dtype=torch.float32, device="cuda")
+    b.get_all_async(cd, xd, vd)
+    torch.cuda.synchronize()
+    tot = int(counts.sum())
+    assert np.array_equal(cd.cpu().numpy().view(np.uint32), counts)
+    assert np.array_equal(xd[:tot].cpu().numpy(), x) and np.array_equal(vd[:tot].cpu().numpy(), v)
+    assert bool((xd[tot:] == -1.0).all())  # nothing written past the live particles
+
+
 def test_pinned_and_pageable_host_buffers_agree(gpu):
     """Packed host buffers in page-locked (pinned) and in pageable memory
     give the same bits, in both directions, around a step."""
