@@ -174,8 +174,9 @@ pbf_status derive_desc(const pbf_params &p, const float domain_end[3], SceneDesc
 
 uint64_t bytes_per_particle(uint32_t max_pair)
 {
-    // x v xs xa xb xold w vt wx (float4) + key slot tmp perm id id_tmp wpos + lam + nnb + selfat + cls + nbr
-    return 9 * 16 + 7 * 4 + 4 + 1 + 1 + 1 + 16ull * ((max_pair - 1 + 3) / 4);  // list slots in whole quads
+    // x v xs xa xb xold w vt wx (float4) + xv (2 float4) + key slot tmp perm id id_tmp wpos + lam + nnb +
+    // selfat + cls + nbr
+    return 11 * 16 + 7 * 4 + 4 + 1 + 1 + 1 + 16ull * ((max_pair - 1 + 3) / 4);  // list slots in whole quads
 }
 
 // ---------------------------------------------------------------- batch --
@@ -187,7 +188,7 @@ Batch::~Batch()
     if (h_small_) cudaFreeHost(h_small_);
     void *ptrs[] = {d_scenes_, d_tile_scene_, d_tile_start_, d_ctrl_, d_scene_num_, d_flags_, d_x_, d_v_,
                     d_xs_, d_xa_, d_xb_, d_xold_, d_w_, d_vt_, d_key_, d_slot_, d_tmp_, d_perm_, d_count_,
-                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_self_, d_bnd_, d_pack_off_, d_active_, d_id_, d_id_tmp_,
+                    d_offsets_, d_bsum_, d_lam_, d_nbr_, d_nnb_, d_self_, d_bnd_, d_pack_off_, d_active_, d_xv_, d_id_, d_id_tmp_,
                     d_next_id_, d_cls_, d_wx_, d_chist_, d_wpos_, d_dense_, d_mid_};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -228,6 +229,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     // + kWalkSpare records: the neighbour walk reads candidates in groups of
     // four and may read up to three past the end of a range (never accepted)
     for (float4 **p : f4) CK(A((void **)p, 16 * (P + kWalkSpare)));
+    CK(A((void **)&d_xv_, 32 * (P + kWalkSpare)));
     uint32_t **u4[] = {&d_key_, &d_slot_, &d_tmp_, &d_perm_, &d_id_, &d_id_tmp_, &d_wpos_};
     for (uint32_t **p : u4) CK(A((void **)p, 4 * P));
     CK(A((void **)&d_count_, 4 * (C + 4)));
@@ -784,6 +786,7 @@ StepArgs Batch::args() const
     a.selfat = d_self_;
     a.w = d_w_;
     a.vt = d_vt_;
+    a.xv = d_xv_;
     a.bnd = d_bnd_;
     a.nbr_stride = max_particles_;
     return a;

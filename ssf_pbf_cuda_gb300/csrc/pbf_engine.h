@@ -153,6 +153,7 @@ private:
     uint32_t *d_next_id_ = nullptr;                   // per scene: next id to hand out
     uint8_t *d_cls_ = nullptr;                        // alias class per particle (input order)
     float4 *d_wx_ = nullptr;                          // class-grouped walk copy of the sorted positions
+    float4 *d_xv_ = nullptr;                          // final (x, v) records, two float4 per particle slot
     uint64_t *d_chist_ = nullptr;                     // per cell: class counts of its bucket
     uint32_t *d_wpos_ = nullptr;                      // sorted slot -> walk-copy slot
     uint32_t *d_dense_ = nullptr;                     // dense-bucket queue

@@ -93,6 +93,8 @@ struct StepArgs {
     uint8_t *nnb;                 // list entries stored (the particle itself is not stored)
     uint8_t *selfat;              // position of the particle itself in its walk-order list, kNotListed if cut
     float4 *w, *vt;               // vorticity, XSPH velocity scratch
+    float4 *xv;                   // final (x, v) side by side, 32 B per particle slot, for the list-form
+                                  // vorticity pass's neighbour gathers (one 256-bit load per neighbour)
     const float4 *bnd;            // boundary primitives
     uint32_t *id, *id_tmp;        // particle ids (phase order) and their sorted copy
     uint8_t *cls;                 // alias class of each particle (input order)

@@ -84,6 +84,15 @@ __device__ __forceinline__ void fma2(float &c0, float &c1, float a0, float a1, f
         : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
 }
 
+// One 32-byte record (two float4) by one 256-bit load through the
+// read-only path; p must be 32-byte aligned.
+__device__ __forceinline__ void ld_rec(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 // r^2 exactly as findPair computes it (pbf_neighbor_search_util.cu:398):
 // fmaf(dz, dz, fmaf(dy, dy, dx * dx)), no further contraction.
 __device__ __forceinline__ float dist2_exact(float4 a, float4 b)
@@ -1563,7 +1572,11 @@ __device__ __forceinline__ void dp_finish(const StepArgs &a, const SceneDesc &d,
     xo[i] = xn;
     if (last) {
         const float4 xo_ = a.xold[i];
-        vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+        const float4 vn =
+            make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+        vo[i] = vn;
+        a.xv[2ull * i] = xn;  // the post passes gather x and v together
+        a.xv[2ull * i + 1] = vn;
         a.id[i] = a.id_tmp[i];  // ids follow the particles into sorted order
     }
 }
@@ -1613,7 +1626,10 @@ __global__ void __launch_bounds__(512) k_finalize(StepArgs a, float4 *__restrict
     const float4 xn = a.xa[i];
     const float4 xo_ = a.xold[i];
     a.x[i] = xn;
-    vo[i] = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+    const float4 vn = make_float4(d.inv_dt * (xn.x - xo_.x), d.inv_dt * (xn.y - xo_.y), d.inv_dt * (xn.z - xo_.z), 0.f);
+    vo[i] = vn;
+    a.xv[2ull * i] = xn;
+    a.xv[2ull * i + 1] = vn;
     a.id[i] = a.id_tmp[i];
     TILE_LOOP_END
 }
@@ -1639,19 +1655,29 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
     const float kh = REF ? d.h : d.inv_h;
     const float4 *__restrict__ x = a.x;
     float w0 = 0.f, w1 = 0.f, w2 = 0.f;
-    auto use = [&](uint32_t j) {
-        const float4 xj = __ldg(x + j);
+    auto pair = [&](const float4 &xj, const float4 &vj) {
         const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
         const float r2 = p0 * p0 + p1 * p1 + p2 * p2;
         if (r2 > 0.f) {
             const float inv_r = rsqrtf(r2);
-            const float4 vj = __ldg(vs + j);
             const float v0 = vj.x - vi.x, v1 = vj.y - vi.y, v2 = vj.z - vi.z;
             const float wd = wspiky_d(r2 * inv_r, kh) * inv_r;
             w0 += (v1 * p2 - v2 * p1) * wd;
             w1 += (v2 * p0 - v0 * p2) * wd;
             w2 += (v0 * p1 - v1 * p0) * wd;
         }
+    };
+    // the walk form gathers x and then, for a pair at r > 0, v
+    auto use = [&](uint32_t j) {
+        const float4 xj = __ldg(x + j);
+        const float p0 = xj.x - xi.x, p1 = xj.y - xi.y, p2 = xj.z - xi.z;
+        if (p0 * p0 + p1 * p1 + p2 * p2 > 0.f) pair(xj, __ldg(vs + j));
+    };
+    // the list form gathers both with one 256-bit load of the (x, v) record
+    auto use_rec = [&](uint32_t j) {
+        float4 xj, vj;
+        ld_rec(a.xv + 2ull * j, xj, vj);
+        pair(xj, vj);
     };
     if (REF) {  // the kernel scaled by h reaches the whole 27-cell block
         walk27_batched(
@@ -1663,7 +1689,7 @@ __global__ void __launch_bounds__(512) k_vort_omega(StepArgs a, const float4 *__
             },
             use);
     } else {
-        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use);
+        list_walk_any<4>(L16, list_of(a.nbr, i), a.nbr_stride, a.nnb[i], d.p_off, use_rec);
     }
     const float mr = d.m * d.inv_rho0;
     const float4 wi = make_float4(mr * w0, mr * w1, mr * w2, 0.f);
