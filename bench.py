@@ -840,7 +840,7 @@ def main():
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk.summary(), "scene_flags_nonzero": sum(1 for f in flags if f),
         }
-        # the figures the benchmark spec's targets are read from, last on the line
+        # the headline ratios (batched and served over plain, serving latency), last on the line
         line["summary"] = {
             "batched": value, "batched_chained": chained["value"] if chained else None,
             "plain": plain["value"] if plain else None,
