@@ -243,7 +243,8 @@ pbf_status pbf_batch_get_all(pbf_batch *b, uint32_t *counts, float *x, float *v,
                              void *stream);
 /* pbf_batch_get_all into device buffers without a host round trip: the
  * packed offsets are computed on the device from the live counts, so the
- * call only enqueues work on the stream.  counts_dev[k] (device memory)
+ * call does not wait for the stream (after scenes were added or removed it
+ * first uploads the scene tables, as pbf_batch_step does).  counts_dev[k] (device memory)
  * receives the k-th active scene's live count; read it once the stream has
  * reached this point.  x_dev / v_dev (either may be NULL) get the same packed
  * layout as pbf_batch_get_all and must hold the active scenes' capacities,
