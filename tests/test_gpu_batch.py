@@ -55,6 +55,30 @@ def test_alone_equals_in_mix_bitwise(gpu):
         assert np.array_equal(x, a["x"]) and np.array_equal(v, a["v"])
 
 
+def test_mixed_list_formats_alone_equals_in_mix(oracle, gpu):
+    """A batch mixing a scene of more than 65,536 slots (u32 neighbour
+    lists) with smaller ones (u16 lists), large enough for the large-step
+    kernels, with the configured XSPH and vorticity list forms (each pass
+    runs once per list format, the vorticity pass gathering (x, v) records):
+    every scene equals itself stepped alone, bit for bit, and the big scene
+    matches the FP64 oracle."""
+    p = api.config_params(scorr_k=1e-4)
+    items = [(scenes.dam_break(40, 40, 44, (4.0, 3.0, 3.0), scene_id=61), p)]
+    items += [(scenes.dam_break(25, 25, 25, (2.0, 2.0, 2.0), scene_id=62 + k), p) for k in range(4)]
+    assert items[0][0].n > 65536 and sum(sc.n for sc, _ in items) > 131072
+    b, ids = make_batch(items)
+    b.step(4)
+    for (sc, pp), sid in zip(items, ids):
+        x, v = b.get_scene(sid)
+        a = alone(sc, pp, 1)
+        assert np.array_equal(x, a["x"]) and np.array_equal(v, a["v"])
+    sc = items[0][0]
+    x, v = b.get_scene(ids[0])
+    r = H.run_oracle(oracle, sc, p, "planes", 4, f64=True)
+    assert H.pos_rel_err(x, r["x"]) <= H.POS_RTOL
+    assert np.abs(v - r["v"]).max(initial=0) <= H.vel_abs_tol(p["time_step"], r["x"])
+
+
 def test_batch_matches_oracle_per_scene(oracle, gpu):
     items = mixed_scenes()
     b, ids = make_batch(items)
