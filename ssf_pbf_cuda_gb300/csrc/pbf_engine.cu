@@ -330,6 +330,7 @@ pbf_status Batch::add_scene(const pbf_params &p, uint32_t capacity, const float 
                             const pbf_boundary_t *b, const float amin[3], const float amax[3], const float *x,
                             const float *v, uint32_t n, bool src_dev, cudaStream_t st, uint32_t *id)
 {
+    NvtxRange range("pbf add scene");
     if (capacity == 0 || n > capacity || !amin || !amax) return PBF_ERROR_INVALID_ARGUMENT;
     if (p.max_pair_particle_num > max_pair_) return PBF_ERROR_INVALID_ARGUMENT;
     SceneHost sh;
@@ -464,6 +465,7 @@ void Batch::scene_ids(std::vector<uint32_t> &ids) const
 
 pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float *v, bool src_dev, cudaStream_t st)
 {
+    NvtxRange range("pbf set all");
     CK(cudaSetDevice(device_));
     std::vector<uint32_t> ids;
     scene_ids(ids);
@@ -514,6 +516,7 @@ pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float
 
 pbf_status Batch::download_all(uint32_t *counts, float *x, float *v, bool dst_dev, cudaStream_t st)
 {
+    NvtxRange range("pbf get all");
     std::vector<uint32_t> nums, fl, ids;
     pbf_status rc = read_all(nums, fl, false, st);
     if (rc != PBF_SUCCESS) return rc;
@@ -549,6 +552,7 @@ pbf_status Batch::download_all(uint32_t *counts, float *x, float *v, bool dst_de
 
 pbf_status Batch::download_all_async(uint32_t *counts_dev, float *x_dev, float *v_dev, cudaStream_t st)
 {
+    NvtxRange range("pbf get all async");
     CK(cudaSetDevice(device_));
     pbf_status rc = upload(st);
     if (rc != PBF_SUCCESS) return rc;
@@ -685,6 +689,7 @@ pbf_status Batch::upload(cudaStream_t st)
         dirty_bnd_ = false;
     }
     if (dirty_tiles_) {
+        NvtxRange range("pbf upload tile lists");
         rebuild_tiles();
         if (tile_scene_.size() > max_tiles_) return PBF_ERROR_CAPACITY;
         if (!tile_scene_.empty()) {
@@ -906,6 +911,7 @@ pbf_status Batch::profile_step(int iters, cudaStream_t st, float *ms, char *name
 
 pbf_status Batch::step(int iters, cudaStream_t st)
 {
+    NvtxRange range("pbf step");
     if (iters < 0 || iters > 1000) return PBF_ERROR_INVALID_ARGUMENT;
     CK(cudaSetDevice(device_));
     pbf_status rc = upload(st);
@@ -1130,6 +1136,7 @@ pbf_status Batch::set_cell_tile(uint32_t cells)
 
 pbf_status Batch::autotune(int iters, cudaStream_t st, uint32_t *chosen)
 {
+    NvtxRange range("pbf autotune");
     CK(cudaSetDevice(device_));
     pbf_status rc = upload(st);
     if (rc != PBF_SUCCESS) return rc;

@@ -4,8 +4,19 @@
 #include <cstdint>
 #include <cstddef>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 namespace pbf103 {
+
+// A named NVTX range on the calling host thread for the life of the object
+// (the host runtime's stages show up on a profiler's timeline; with no
+// profiler attached a range costs a function-pointer test).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Per-scene constants, one 240-byte record per scene slot in device memory.
 // Derived once on the host from pbf_params (the reference keeps these in

@@ -74,6 +74,7 @@ struct pbf_server {
 
 pbf_status pbf_server::service(bool *did_work)
 {
+    NvtxRange range("pbf serve round");
     *did_work = false;
     // admit in arrival order while the budget and the arena allow
     for (;;) {
