@@ -650,8 +650,9 @@ def main():
         # results device -> host (pinned host buffers).  The copies run on a
         # copy stream through device staging buffers (two for the inputs), so
         # step k+1's upload and step k-1's download overlap step k's compute;
-        # the compute stream runs pbf_batch_set_all from the staged inputs,
-        # the step and pbf_batch_get_all_async into the staged outputs (the
+        # the compute stream runs pbf_batch_step_packed on the staged inputs
+        # (set_all and the step in one call, the step reading the packed
+        # input where it lies) and pbf_batch_get_all_async into the staged outputs (the
         # packed offsets computed on the device: the host never waits for a
         # step, only for a staging buffer to come free).
         xh = torch.from_numpy(x0h).pin_memory()
@@ -676,8 +677,7 @@ def main():
 
         def compute(k):
             stream.wait_event(in_ready[k % 2])
-            batch.set_all(xin[k % 2], vin[k % 2], counts, stream)
-            batch.step(ITERS, stream)
+            batch.step_packed(ITERS, xin[k % 2], vin[k % 2], counts, stream)  # set_all + step, no unpack pass
 
         def download():
             stream.wait_event(out_free)  # the previous download has left the staging buffer
@@ -717,7 +717,7 @@ def main():
                "ms_per_step": dt / args.steps * 1e3,
                "pipeline": "one batch; host->device and device->host copies of pinned buffers on a copy "
                            "stream through device staging, overlapping the neighbouring steps' compute; "
-                           "pbf_batch_set_all / step / get_all_async on the compute stream, no host wait "
+                           "pbf_batch_step_packed / get_all_async on the compute stream, no host wait "
                            "on a step"}
         assert int(co.numpy().view(np.uint32).sum()) > 0
         del xin, vin, xout, vout, cout

@@ -241,6 +241,15 @@ pbf_status pbf_batch_set_all(pbf_batch *b, const uint32_t *counts, const float *
                              int src_is_device, void *stream);
 pbf_status pbf_batch_get_all(pbf_batch *b, uint32_t *counts, float *x, float *v, int dst_is_device,
                              void *stream);
+/* pbf_batch_set_all from device buffers followed by pbf_batch_step, in one
+ * call without the unpack pass: the step's first passes read the packed
+ * positions and velocities (scenes back to back in scene-id order, counts
+ * as pbf_batch_set_all's) where they lie.  x_dev / v_dev (v_dev NULL: zero
+ * velocities) must stay unchanged until the stream has run the step.  The
+ * result is bit for bit that of pbf_batch_set_all + pbf_batch_step, and the
+ * batch holds it as after pbf_batch_step.  No reference counterpart. */
+pbf_status pbf_batch_step_packed(pbf_batch *b, int iters, const uint32_t *counts, const float *x_dev,
+                                 const float *v_dev, void *stream);
 /* pbf_batch_get_all into device buffers without a host round trip: the
  * packed offsets are computed on the device from the live counts, so the
  * call does not wait for the stream (after scenes were added or removed it

@@ -132,6 +132,7 @@ SIGNATURES = {
     "pbf_batch_scene_ids": (c_i32, [c_vp, P(c_u32), c_u32, P(c_u32)]),
     "pbf_batch_set_all": (c_i32, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int, c_vp]),
     "pbf_batch_get_all": (c_i32, [c_vp, c_vp, c_vp, c_vp, ctypes.c_int, c_vp]),
+    "pbf_batch_step_packed": (c_i32, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]),
     "pbf_batch_get_all_async": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp]),
     "pbf_batch_autotune": (c_i32, [c_vp, ctypes.c_int, c_vp, P(c_u32)]),
     "pbf_batch_set_tile": (c_i32, [c_vp, c_u32]),

@@ -543,6 +543,16 @@ class Batch:
                                        _stream(stream)), "pbf_batch_get_all")
         return counts[:len(ids)], x_out, v_out
 
+    def step_packed(self, iters: int, x_dev, v_dev=None, counts=None, stream=None):
+        """set_all from device buffers and step in one call, the step reading
+        the packed input where it lies (no unpack pass)."""
+        c = None
+        if counts is not None:
+            c = np.ascontiguousarray(np.asarray(counts, np.uint32))
+            self._counts_keep = c
+        check(load().pbf_batch_step_packed(self.handle, int(iters), c.ctypes.data if c is not None else None,
+                                           _ptr(x_dev), _ptr(v_dev), _stream(stream)), "pbf_batch_step_packed")
+
     def get_all_async(self, counts_dev, x_dev=None, v_dev=None, stream=None):
         """Download every active scene into device buffers (packed as get_all)
         without waiting for the stream: counts_dev (device uint32, one per

@@ -461,6 +461,16 @@ pbf_status pbf_batch_get_all(pbf_batch *b, uint32_t *counts, float *x, float *v,
     return b->b.download_all(counts, x, v, dst_dev != 0, S(st));
 }
 
+pbf_status pbf_batch_step_packed(pbf_batch *b, int iters, const uint32_t *counts, const float *x_dev,
+                                 const float *v_dev, void *st)
+{
+    if (!b) return PBF_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(b->mu);
+    pbf_status rc = set_dev(b->b.device());
+    if (rc) return rc;
+    return b->b.step_packed(iters, counts, x_dev, v_dev, S(st));
+}
+
 pbf_status pbf_batch_get_all_async(pbf_batch *b, uint32_t *counts_dev, float *x_dev, float *v_dev, void *st)
 {
     if (!b || !counts_dev) return PBF_ERROR_INVALID_ARGUMENT;

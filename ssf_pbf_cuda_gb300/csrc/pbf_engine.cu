@@ -182,7 +182,9 @@ uint64_t bytes_per_particle(uint32_t max_pair)
 // ---------------------------------------------------------------- batch --
 Batch::~Batch()
 {
-    if (exec_) cudaGraphExecDestroy(exec_);
+    for (cudaGraphExec_t e : exec_)
+        if (e) cudaGraphExecDestroy(e);
+    if (d_pin_) cudaFree(d_pin_);
     if (cap_stream_) cudaStreamDestroy(cap_stream_);
     if (small_done_) cudaEventDestroy(small_done_);
     if (h_small_) cudaFreeHost(h_small_);
@@ -246,6 +248,7 @@ pbf_status Batch::init(uint32_t max_scenes, uint64_t max_particles, uint64_t max
     CK(A((void **)&d_bnd_, 16 * bnd_capacity_));
     CK(A((void **)&d_pack_off_, 4ull * max_scenes));
     CK(A((void **)&d_active_, 4ull * max_scenes));
+    CK(A((void **)&d_pin_, sizeof(PackedIn)));
     CK(cudaMallocHost((void **)&h_small_, 8ull * max_scenes + 64));
     CK(cudaEventCreateWithFlags(&small_done_, cudaEventDisableTiming));
     CK(cudaMemset(d_count_, 0, 4 * (C + 4)));
@@ -471,6 +474,30 @@ pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float
     scene_ids(ids);
     if (ids.empty()) return PBF_SUCCESS;
     if (!x) return PBF_ERROR_INVALID_ARGUMENT;
+    pbf_status rc = stage_counts(counts, ids, st);
+    if (rc != PBF_SUCCESS) return rc;
+    uint64_t tot = 0;
+    for (uint32_t id : ids) tot += scenes_[id].num_upper;
+    const float *sx = x, *sv = v;
+    if (!src_dev && tot) {
+        CK(cudaMemcpyAsync(d_xs_, x, 12 * tot, cudaMemcpyHostToDevice, st));
+        sx = reinterpret_cast<const float *>(d_xs_);
+        if (v) {
+            CK(cudaMemcpyAsync(d_vt_, v, 12 * tot, cudaMemcpyHostToDevice, st));
+            sv = reinterpret_cast<const float *>(d_vt_);
+        }
+    }
+    if (ctrl_.n_tiles) launch_unpack(args(), shape_for(tile_), d_pack_off_, sx, sv, st);
+    CK(cudaGetLastError());
+    // k_unpack restarts the id counters of scenes with particles; the rest here
+    for (size_t k = 0; k < ids.size(); ++k)
+        if (scenes_[ids[k]].num_upper == 0) launch_set_u32(d_next_id_ + ids[k], 0, st);
+    CK(cudaGetLastError());
+    return PBF_SUCCESS;
+}
+
+pbf_status Batch::stage_counts(const uint32_t *counts, const std::vector<uint32_t> &ids, cudaStream_t st)
+{
     for (size_t k = 0; k < ids.size(); ++k) {
         const uint32_t c = counts ? counts[k] : scenes_[ids[k]].num_upper;
         if (c > scenes_[ids[k]].desc.capacity) return PBF_ERROR_CAPACITY;
@@ -494,24 +521,36 @@ pbf_status Batch::upload_all(const uint32_t *counts, const float *x, const float
     CK(cudaMemcpyAsync(d_pack_off_, pack, 4 * ns, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_scene_num_, nums, 4 * ns, cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(small_done_, st));
-    pbf_status rc = upload(st);
-    if (rc != PBF_SUCCESS) return rc;
-    const float *sx = x, *sv = v;
-    if (!src_dev && tot) {
-        CK(cudaMemcpyAsync(d_xs_, x, 12 * tot, cudaMemcpyHostToDevice, st));
-        sx = reinterpret_cast<const float *>(d_xs_);
-        if (v) {
-            CK(cudaMemcpyAsync(d_vt_, v, 12 * tot, cudaMemcpyHostToDevice, st));
-            sv = reinterpret_cast<const float *>(d_vt_);
-        }
+    return upload(st);
+}
+
+pbf_status Batch::step_packed(int iters, const uint32_t *counts, const float *x, const float *v, cudaStream_t st)
+{
+    NvtxRange range("pbf step packed");
+    if (iters < 0 || iters > 1000) return PBF_ERROR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(device_));
+    std::vector<uint32_t> ids;
+    scene_ids(ids);
+    if (ids.empty()) {
+        last_launches_ = 0;
+        return PBF_SUCCESS;
     }
-    if (ctrl_.n_tiles) launch_unpack(args(), shape_for(tile_), d_pack_off_, sx, sv, st);
+    if (!x) return PBF_ERROR_INVALID_ARGUMENT;
+    pbf_status rc = stage_counts(counts, ids, st);
+    if (rc != PBF_SUCCESS) return rc;
+    // the prediction restarts the id counters of scenes with particles; the rest here
+    for (uint32_t id : ids)
+        if (scenes_[id].num_upper == 0) launch_set_u32(d_next_id_ + id, 0, st);
+    if (ctrl_.n_tiles == 0) {
+        last_launches_ = 0;
+        return PBF_SUCCESS;
+    }
+    launch_set_packed_in(d_pin_, x, v, st);
     CK(cudaGetLastError());
-    // k_unpack restarts the id counters of scenes with particles; the rest here
-    for (size_t k = 0; k < ids.size(); ++k)
-        if (scenes_[ids[k]].num_upper == 0) launch_set_u32(d_next_id_ + ids[k], 0, st);
-    CK(cudaGetLastError());
-    return PBF_SUCCESS;
+    rc = run(iters, st, true, true);
+    if (rc == PBF_SUCCESS)
+        for (auto &s : scenes_) s.perm_valid = s.active;
+    return rc;
 }
 
 pbf_status Batch::download_all(uint32_t *counts, float *x, float *v, bool dst_dev, cudaStream_t st)
@@ -794,6 +833,8 @@ StepArgs Batch::args() const
     a.xv = d_xv_;
     a.bnd = d_bnd_;
     a.nbr_stride = max_particles_;
+    a.pin = d_pin_;
+    a.pack_off = d_pack_off_;
     return a;
 }
 
@@ -822,37 +863,38 @@ uint32_t Batch::post_modes() const
     return m;
 }
 
-pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph)
+pbf_status Batch::run(int iters, cudaStream_t st, bool allow_graph, bool packed)
 {
     const LaunchShape sh = shape_for(tile_);
     const uint32_t modes = post_modes();
+    const int f = packed ? 1 : 0;
     if (allow_graph && graph_mode_) {
         GraphKey k;
         k.iters = iters;
         k.modes = modes;
         k.shape = sh;
-        if (!exec_ || !(k == key_)) {
-            if (exec_) {
-                cudaGraphExecDestroy(exec_);
-                exec_ = nullptr;
+        if (!exec_[f] || !(k == key_[f])) {
+            if (exec_[f]) {
+                cudaGraphExecDestroy(exec_[f]);
+                exec_[f] = nullptr;
             }
             CK(cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeThreadLocal));
-            graph_launches_ = enqueue_step(args(), sh, iters, modes, cap_stream_);
+            graph_launches_[f] = enqueue_step(args(), sh, iters, modes, cap_stream_, nullptr, packed);
             cudaGraph_t g = nullptr;
             CK(cudaStreamEndCapture(cap_stream_, &g));
-            cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
+            cudaError_t e = cudaGraphInstantiate(&exec_[f], g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) {
-                exec_ = nullptr;
+                exec_[f] = nullptr;
                 set_last_error("cudaGraphInstantiate", e);
                 return PBF_ERROR_CUDA;
             }
-            key_ = k;
+            key_[f] = k;
         }
-        CK(cudaGraphLaunch(exec_, st));
-        last_launches_ = graph_launches_;
+        CK(cudaGraphLaunch(exec_[f], st));
+        last_launches_ = graph_launches_[f];
     } else {
-        last_launches_ = enqueue_step(args(), sh, iters, modes, st);
+        last_launches_ = enqueue_step(args(), sh, iters, modes, st, nullptr, packed);
     }
     CK(cudaGetLastError());
     return PBF_SUCCESS;

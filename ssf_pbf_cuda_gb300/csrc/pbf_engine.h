@@ -66,6 +66,9 @@ public:
     pbf_status set_scene_boundary(uint32_t id, const pbf_boundary_t *b);
     pbf_status set_scene_area(uint32_t id, const float amin[3], const float amax[3]);
     pbf_status step(int iters, cudaStream_t st);
+    // upload_all from device buffers and step, without the unpack pass: the
+    // step reads the packed input where it lies
+    pbf_status step_packed(int iters, const uint32_t *counts, const float *x, const float *v, cudaStream_t st);
     pbf_status get_num(uint32_t id, uint32_t *num, cudaStream_t st);
     pbf_status get_particles(uint32_t id, float *x, float *v, uint32_t *num, bool dst_dev, cudaStream_t st);
     pbf_status get_flags(uint32_t id, uint32_t *flags, bool clear, cudaStream_t st);
@@ -119,7 +122,9 @@ public:
 
 private:
     pbf_status upload(cudaStream_t st);
-    pbf_status run(int iters, cudaStream_t st, bool allow_graph);
+    pbf_status run(int iters, cudaStream_t st, bool allow_graph, bool packed = false);
+    // set the active scenes' counts (or keep them) and stage their pack offsets
+    pbf_status stage_counts(const uint32_t *counts, const std::vector<uint32_t> &ids, cudaStream_t st);
     LaunchShape shape_for(uint32_t tile) const;
     uint32_t post_modes() const;  // kPost* bits of the active scenes
     void rebuild_tiles();
@@ -177,7 +182,6 @@ private:
     uint32_t cell_tile_ = kCellTile;
     bool graph_mode_ = true;
     cudaStream_t cap_stream_ = nullptr;
-    cudaGraphExec_t exec_ = nullptr;
     struct GraphKey {
         int iters = -1;
         uint32_t modes = 0;
@@ -186,9 +190,13 @@ private:
         {
             return iters == o.iters && modes == o.modes && shape == o.shape;
         }
-    } key_;
+    };
+    // one captured step per input form: [0] the phase, [1] packed input
+    cudaGraphExec_t exec_[2] = {nullptr, nullptr};
+    GraphKey key_[2];
+    uint32_t graph_launches_[2] = {0, 0};
     uint32_t last_launches_ = 0;
-    uint32_t graph_launches_ = 0;
+    PackedIn *d_pin_ = nullptr;  // input buffers of the current packed-input step
 };
 
 }  // namespace pbf103

@@ -87,6 +87,13 @@ struct Ctrl {
     uint32_t n_cell_tiles;  // cell tiles after them: LaunchShape::cell_tile cells of one scene each
 };
 
+// Device-resident pointers to a step's packed AoS float3 input
+// (pbf_batch_step_packed): set by a one-thread kernel before each such step,
+// so a captured graph reads whichever buffers the call names.
+struct PackedIn {
+    const float *x, *v;  // v may be null (zero velocities)
+};
+
 struct StepArgs {
     const SceneDesc *scenes;
     const uint32_t *tile_scene;   // tile -> scene
@@ -116,6 +123,8 @@ struct StepArgs {
     uint64_t *chist;              // per cell: 8 x 8-bit class counts of its bucket, or kClassWhole
     uint32_t *next_id;            // per scene: id of the next particle added
     uint64_t nbr_stride;
+    const PackedIn *pin;          // packed-input steps: the input buffers
+    const uint32_t *pack_off;     // packed-input steps: first packed particle of each scene
 };
 
 struct LaunchShape {
@@ -166,8 +175,12 @@ enum : uint32_t {
 
 // Enqueue one full solver step for every scene in the tile list.
 // Returns the number of kernels launched.
+// packed: the step reads its input positions and velocities from the packed
+// AoS float3 buffers named in *a.pin (scene s from a.pack_off[s]) instead of
+// the particle phase, and numbers the particles afresh, as an upload does.
 uint32_t enqueue_step(const StepArgs &a, const LaunchShape &s, int iters, uint32_t post_modes,
-                      cudaStream_t stream, StepHook *hook = nullptr);
+                      cudaStream_t stream, StepHook *hook = nullptr, bool packed = false);
+void launch_set_packed_in(PackedIn *dst, const float *x, const float *v, cudaStream_t st);
 
 // Edge conversions between the ABI's AoS float3 and the internal float4.
 void launch_aos3_to_f4(const float *src, float4 *dst, uint32_t n, cudaStream_t st);

@@ -596,6 +596,10 @@ __device__ __forceinline__ void list_walk_ahead2(const uint32_t *__restrict__ nl
 // calcHash (pbf_neighbor_search_util.cu:20-37), checkDeleteParticle
 // (pbf_delete.cu:9-28; deleted key = ncell, one past the last cell) and the
 // histogram of countingSort (insertAndCountCUDA, pbf_counting_sort.cu:21-32).
+// PACKED: the input phase is read from the packed AoS float3 buffers of a
+// packed-input step (what k_unpack would have written), and the particles
+// are numbered afresh.
+template <bool PACKED>
 __global__ void __launch_bounds__(512) k_predict_hash(StepArgs a)
 {
     TILE_LOOP_BEGIN
@@ -603,14 +607,26 @@ __global__ void __launch_bounds__(512) k_predict_hash(StepArgs a)
     if (local >= n) continue;
     const SceneDesc d = a.scenes[s];
     const uint32_t i = d.p_off + local;
-    const float4 xv = a.x[i];
-    const float4 vv = a.v[i];
+    float4 xv, vv;
+    uint32_t id;
+    if (PACKED) {
+        const PackedIn pin = *a.pin;
+        const uint64_t q = 3ull * ((uint64_t)a.pack_off[s] + local);
+        xv = make_float4(pin.x[q], pin.x[q + 1], pin.x[q + 2], 0.f);
+        vv = pin.v ? make_float4(pin.v[q], pin.v[q + 1], pin.v[q + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        id = local;
+        if (local == 0) a.next_id[s] = n;
+    } else {
+        xv = a.x[i];
+        vv = a.v[i];
+        id = a.id[i];
+    }
     const float dt = d.dt;
     float4 ps;
     ps.x = __fmaf_rn(__fmaf_rn(d.g[0], dt, vv.x), dt, xv.x);
     ps.y = __fmaf_rn(__fmaf_rn(d.g[1], dt, vv.y), dt, xv.y);
     ps.z = __fmaf_rn(__fmaf_rn(d.g[2], dt, vv.z), dt, xv.z);
-    ps.w = __uint_as_float(a.id[i]);  // the id travels with the prediction to k_gather
+    ps.w = __uint_as_float(id);  // the id travels with the prediction to k_gather
     const int32_t cx = cell_coord(ps.x, d.cw), cy = cell_coord(ps.y, d.cw), cz = cell_coord(ps.z, d.cw);
     uint32_t key = hash3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz, d);
     uint32_t cls = alias_class(cx, cy, cz, d);
@@ -1118,7 +1134,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_dense_sort(StepArgs a)
 // Reorder in sorted order (reorderDataCUDA x2, pbf_neighbor_search_util.cu:143-154):
 // sorted predicted positions (carrying their own slot in .w, which the
 // neighbour walk records), sorted old positions and ids; the walk copy of
-// mixed-class buckets.
+// mixed-class buckets.  PACKED: old positions from the packed input.
+template <bool PACKED>
 __global__ void __launch_bounds__(512) k_gather(StepArgs a)
 {
     TILE_LOOP_BEGIN
@@ -1126,11 +1143,17 @@ __global__ void __launch_bounds__(512) k_gather(StepArgs a)
     if (local >= n) continue;
     const SceneDesc d = a.scenes[s];
     const uint32_t g = d.p_off + local;
-    const uint32_t i = d.p_off + a.perm[g];
+    const uint32_t li = a.perm[g];
+    const uint32_t i = d.p_off + li;
     const float4 ps = a.xs[i];
     const float4 xg = make_float4(ps.x, ps.y, ps.z, __uint_as_float(g));
     a.xa[g] = xg;
-    a.xold[g] = a.x[i];
+    if (PACKED) {
+        const float *px = a.pin->x + 3ull * ((uint64_t)a.pack_off[s] + li);
+        a.xold[g] = make_float4(px[0], px[1], px[2], 0.f);
+    } else {
+        a.xold[g] = a.x[i];
+    }
     a.id_tmp[g] = __float_as_uint(ps.w);  // the id, stored beside the prediction
     const uint32_t w = a.wpos[g];
     if (w != kNoWalkCopy) a.wx[w] = xg;
@@ -1986,8 +2009,11 @@ Occupancy occupancy(uint32_t tile, uint32_t chunk)
     auto occ = [&](const void *fn) { return occ_b(fn, tile); };
     auto mn = [](uint32_t a, uint32_t b) { return a < b ? a : b; };
     Occupancy o;
-    o.light = mn(mn(occ((const void *)k_predict_hash), occ((const void *)k_scatter)),
-                 mn(mn(occ((const void *)k_rank_reorder), occ((const void *)k_gather)), occ((const void *)k_finalize)));
+    o.light = mn(mn(mn(occ((const void *)k_predict_hash<false>), occ((const void *)k_predict_hash<true>)),
+                    occ((const void *)k_scatter)),
+                 mn(mn(occ((const void *)k_rank_reorder), mn(occ((const void *)k_gather<false>),
+                                                             occ((const void *)k_gather<true>))),
+                    occ((const void *)k_finalize)));
     o.cells = occ_b((const void *)k_rank_cells, kCellTileMax);
     o.split = occ_b((const void *)k_neighbors_split, 256);
     o.nb = occ((const void *)k_neighbors_lambda<false>);
@@ -2034,8 +2060,15 @@ void launch_pack(const StepArgs &a, const LaunchShape &sh, const uint32_t *pack_
     k_pack<<<sh.grid, sh.tile, 0, st>>>(a, pack_off, dst_x, dst_v);
 }
 
+__global__ void k_set_packed_in(PackedIn *dst, const float *x, const float *v) { *dst = PackedIn{x, v}; }
+
+void launch_set_packed_in(PackedIn *dst, const float *x, const float *v, cudaStream_t st)
+{
+    k_set_packed_in<<<1, 1, 0, st>>>(dst, x, v);
+}
+
 uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint32_t post,
-                      cudaStream_t st, StepHook *hook)
+                      cudaStream_t st, StepHook *hook, bool packed)
 {
     uint32_t nl = 0;
     const dim3 g(sh.grid), b(sh.tile);
@@ -2044,7 +2077,10 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
         ++nl;                             \
         if (hook) hook->launched(name);   \
     } while (0)
-    k_predict_hash<<<g, b, 0, st>>>(a);
+    if (packed)
+        k_predict_hash<true><<<g, b, 0, st>>>(a);
+    else
+        k_predict_hash<false><<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_predict_hash");
     if (sh.scan_grid == 0) {  // small table: one block
         switch (sh.scan_rounds) {  // rounds of 1024 cells held in registers
@@ -2077,7 +2113,10 @@ uint32_t enqueue_step(const StepArgs &a, const LaunchShape &sh, int iters, uint3
     }
     k_dense_sort<<<sh.grid, kRadixThreads, 0, st>>>(a);
     PBF_LAUNCHED("k_dense_sort");
-    k_gather<<<g, b, 0, st>>>(a);
+    if (packed)
+        k_gather<true><<<g, b, 0, st>>>(a);
+    else
+        k_gather<false><<<g, b, 0, st>>>(a);
     PBF_LAUNCHED("k_gather");
     if (sh.small) {
         k_neighbors_split<<<sh.grid_split, 256, 0, st>>>(a, sh.tile);

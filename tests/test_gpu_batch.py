@@ -208,6 +208,41 @@ def test_get_all_async_equals_get_all(gpu):
     assert bool((xd[tot:] == -1.0).all())  # nothing written past the live particles
 
 
+def test_step_packed_equals_set_all_then_step(gpu):
+    """pbf_batch_step_packed (the step reading its packed input where it lies,
+    no unpack pass) gives bit for bit what pbf_batch_set_all from the same
+    device buffers followed by pbf_batch_step gives: counts, positions,
+    velocities and particle ids, over two steps from two different input
+    buffers (the second without velocities), with a removed scene's slot and
+    a scene whose area deletes particles."""
+    import dataclasses
+    import torch
+    items = mixed_scenes()
+    sc = scenes.dam_break(12, 12, 12, (1.5, 1.5, 1.5), scene_id=53)
+    items.append((dataclasses.replace(sc, area=((-0.1, -0.1, -0.1), (1.6, 0.45, 1.6))),
+                  api.config_params(scorr_k=1e-4)))
+    keep = [k for k in range(len(items)) if k != 1]
+    counts = [items[k][0].n for k in keep]
+    x = np.concatenate([items[k][0].x for k in keep]).astype(np.float32)
+    v = np.concatenate([items[k][0].v for k in keep]).astype(np.float32)
+    inputs = [(torch.from_numpy(x).cuda(), torch.from_numpy(v).cuda()),
+              (torch.from_numpy(x + np.float32(0.002)).cuda(), None)]
+    b1, ids1 = make_batch(items)
+    b2, ids2 = make_batch(items)
+    b1.remove_scene(ids1[1])
+    b2.remove_scene(ids2[1])
+    for xd, vd in inputs:
+        b1.set_all(xd, vd, counts)
+        b1.step(4)
+        b2.step_packed(4, xd, vd, counts)
+        c1, x1, v1 = b1.get_all()
+        c2, x2, v2 = b2.get_all()
+        assert np.array_equal(c1, c2) and c1[-1] < counts[-1]
+        assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
+        for k in keep:
+            assert np.array_equal(b1.particle_ids(ids1[k]), b2.particle_ids(ids2[k]))
+
+
 def test_pinned_and_pageable_host_buffers_agree(gpu):
     """Packed host buffers in page-locked (pinned) and in pageable memory
     give the same bits, in both directions, around a step."""
