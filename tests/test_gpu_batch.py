@@ -208,13 +208,15 @@ def test_get_all_async_equals_get_all(gpu):
     assert bool((xd[tot:] == -1.0).all())  # nothing written past the live particles
 
 
-def test_step_packed_equals_set_all_then_step(gpu):
+@pytest.mark.parametrize("graph", [True, False], ids=["graph", "no_graph"])
+def test_step_packed_equals_set_all_then_step(gpu, graph):
     """pbf_batch_step_packed (the step reading its packed input where it lies,
     no unpack pass) gives bit for bit what pbf_batch_set_all from the same
     device buffers followed by pbf_batch_step gives: counts, positions,
     velocities and particle ids, over two steps from two different input
     buffers (the second without velocities), with a removed scene's slot and
-    a scene whose area deletes particles."""
+    a scene whose area deletes particles; captured in a graph or launched
+    kernel by kernel."""
     import dataclasses
     import torch
     items = mixed_scenes()
@@ -231,6 +233,7 @@ def test_step_packed_equals_set_all_then_step(gpu):
     b2, ids2 = make_batch(items)
     b1.remove_scene(ids1[1])
     b2.remove_scene(ids2[1])
+    b2.set_graph_mode(graph)
     for xd, vd in inputs:
         b1.set_all(xd, vd, counts)
         b1.step(4)
