@@ -77,14 +77,22 @@ def test_mass_deletion_is_sorted_stably(oracle, gpu, n):
 
 
 def test_config2_single_large_step_properties(oracle, gpu):
-    """1,048,576 particles, 2^21-cell table: the integer pipeline is bit-exact
-    against the oracle and the permutation is a permutation."""
+    """1,048,576 particles, 2^21-cell table, the configured physics: the
+    integer pipeline is bit-exact against the oracle, the permutation is a
+    permutation, and after one step of one solver iteration (where the
+    configured physics is still well conditioned) positions are within 1e-5
+    relative and velocities within that error over dt of both the FP32 and
+    the FP64 oracle."""
     sc = scenes.config2()
     params = api.config_params()
     g = H.run_gpu(sc, params, "planes", iters=1)
     r = H.run_oracle(oracle, sc, params, "planes", iters=1)
     H.assert_integer_parity(g, r, H.resolved(params, sc))
     assert np.array_equal(np.sort(g["perm"]), np.arange(sc.n, dtype=np.uint32))
+    r64 = H.run_oracle(oracle, sc, params, "planes", iters=1, f64=True)
+    for ref in (r, r64):
+        assert H.pos_rel_err(g["x"], ref["x"]) <= H.POS_RTOL
+        assert np.abs(g["v"] - ref["v"]).max(initial=0) <= H.vel_abs_tol(params["time_step"], ref["x"])
 
 
 def _kinetic(p, v):
