@@ -77,6 +77,23 @@ def test_config4_slice_one_iteration(oracle, gpu):
             _assert_close(x, v, H.run_oracle(oracle, sc, p, "planes", 1, f64=f64), p["time_step"])
 
 
+def test_config4_full_one_iteration(oracle, gpu):
+    """The whole batched workload (256 scenes, 5,710,854 particles) in one
+    batch, stepped through the packed-input step the benchmark times: every
+    scene within 1e-5 relative of the FP32 and of the FP64 oracle after one
+    iteration."""
+    import torch
+    items = [(sc, api.config_params()) for sc in scenes.config4(256)]
+    b, ids = _batch(items)
+    x = torch.from_numpy(np.concatenate([sc.x for sc, _ in items]).astype(np.float32)).cuda()
+    v = torch.from_numpy(np.concatenate([sc.v for sc, _ in items]).astype(np.float32)).cuda()
+    b.step_packed(1, x, v, [sc.n for sc, _ in items])
+    for (sc, p), sid in zip(items, ids):
+        xg, vg = b.get_scene(sid)
+        for f64 in (False, True):
+            _assert_close(xg, vg, H.run_oracle(oracle, sc, p, "planes", 1, f64=f64), p["time_step"])
+
+
 def test_config4_slice_four_iterations(oracle, gpu):
     items = _slice4()
     b, ids = _batch(items)
